@@ -1,0 +1,367 @@
+"""Benchmark: Mrays/s of the path tracer on the large single-mesh workload.
+
+Workload (one GPU): a displaced icosphere of 1,310,720 triangles (level-8
+subdivision, seeded 6-octave value noise of amplitude 0.08 r, dielectric
+n = 1.5) inside the Cornell box, 1024 x 1024 pixels, 8 bounces, compat
+estimator.  One step = one progressive launch of 16 samples per pixel over
+the whole frame (16 steps = the 256-spp frame), inputs resident in HBM.
+
+Metric: rays actually traced (primary + bounce + shadow) per second of
+device time, in millions.  Multi-GPU: each rank renders its own disjoint
+range of sample indices of the same frame (weak scaling, no collective on
+the data path; a barrier and a max-reduce of the time only).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference estimator's CPU restatement (the
+oracle: LiSA's own GPU path is OptiX and does not build here) on all host
+cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("displaced icosphere 1,310,720 tris (dielectric n=1.5) in Cornell box, 1024x1024, 8 bounces, "
+            "16 spp per step (256-spp frame = 16 steps), compat estimator")
+METRIC = "Mrays/s (primary+bounce+shadow rays traced)"
+
+
+def dist_init(gpus: int):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, ws, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x: float, ws: int) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the emitter-search kernel from the committed
+    ncu summary (profiles/nee_traffic.txt, key=value lines), or None."""
+    p = os.path.join(ROOT, "profiles", "nee_traffic.txt")
+    try:
+        kv = {}
+        with open(p) as f:
+            for ln in f:
+                if "=" in ln and not ln.startswith("#"):
+                    k, v = ln.split("=", 1)
+                    kv[k.strip()] = v.strip()
+        return float(kv["dram_bytes_per_vertex"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def make_scene(level=8):
+    from lisa_gb300 import scenes
+
+    return scenes.icosphere_box(level=level, width=1024, height=1024, num_samples=256, num_bounces=8)
+
+
+# algorithmic bytes of the emitter-search kernel (k_nee): per opaque vertex
+# the queue entry (48 B) + path state read and written back (36 + 36 B) + the
+# continuation ray (32 B); per shadow ray the material look-up of the hit
+# (16 B); per node visit 80 B; per triangle test 48 B.
+NEE_B_VERTEX = 48 + 36 + 36 + 32
+NEE_B_RAY = 16
+B_NODE = 80
+B_TRI = 48
+
+
+def cpu_sample(scene, spp, budget_s=12.0, threads=0, seed=0):
+    """Time the CPU oracle on a bounded sample of the workload: bands of
+    pixels spread over the frame, `spp` samples each.  Returns (Mrays/s,
+    description, cores)."""
+    import oracle as O
+
+    osc = O.Scene.from_scene(scene, spp=spp, seed=seed)
+    osc.render(0, 1, use_bvh=True, threads=threads)  # builds the CPU BVH once
+    w, h = scene.width, scene.height
+    cores = threads or os.cpu_count()
+    npx = 64
+    rays_tot, t_tot, px_tot = 0, 0.0, 0
+    bands = 0
+    for y in np.linspace(0, h - 1, 64).astype(int).tolist():
+        x0 = (bands * 97) % (w - npx)
+        p0 = y * w + x0
+        t0 = time.perf_counter()
+        _, _, rays = osc.render(p0, p0 + npx, use_bvh=True, threads=threads)
+        t_tot += time.perf_counter() - t0
+        rays_tot += int(rays.sum())
+        px_tot += npx
+        bands += 1
+        if t_tot > budget_s:
+            break
+    # the BVH build of the oracle is repeated per call; subtract it by timing an empty call
+    t0 = time.perf_counter()
+    osc.render(0, 0, use_bvh=True, threads=threads)
+    build = time.perf_counter() - t0
+    t_net = max(t_tot - bands * build, 1e-9)
+    return rays_tot / t_net / 1e6, f"{px_tot} pixels in {bands} bands x {spp} spp of the same frame", cores
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    sc = make_scene()
+    vals = []
+    desc, cores = "", os.cpu_count()
+    for i in range(args.warmup + args.steps):
+        v, desc, cores = cpu_sample(sc, spp=args.spp_per_step, budget_s=args.ref_budget, seed=i)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "l2": "host-side run"},
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, ws, local):
+    import torch
+
+    import lisa_gb300 as L
+
+    sc = make_scene()
+    params = L.params_from_scene(sc)
+    opts = L.default_options(stage_timing=1, seed=1000 * rank, paths_in_flight=args.paths)
+    r = L.Renderer(params, opts)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def step():
+        flush.zero_()
+        torch.cuda.synchronize()
+        return r.render_progressive(args.spp_per_step)
+
+    for _ in range(args.warmup):
+        step()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    t0 = time.perf_counter()
+    stats = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    barrier(ws)
+    dev_s = sum(s.ms_device for s in stats) / 1e3
+    rays = sum(s.rays for s in stats)
+    t_max = max_over_ranks(dev_s, ws)
+    rays_all = sum_over_ranks(float(rays), ws)
+    value = rays_all / t_max / 1e6
+    # dominant kernel: the emitter search (k_nee); per-launch device time
+    nee_ms = sum(s.ms_nee for s in stats)
+    nee_launches = sum(s.launches_nee for s in stats)
+    trace_ms = sum(s.ms_trace for s in stats)
+    shade_ms = sum(s.ms_shade for s in stats)
+    other_ms = sum(s.ms_other for s in stats)
+    launches = sum(s.launches_total for s in stats)
+    # counting pass (same seeds, one step) for the algorithmic bytes per launch
+    copts = L.default_options(seed=1000 * rank, paths_in_flight=args.paths, count_traversal=1)
+    rc = L.Renderer(params, copts)
+    cs = rc.render_progressive(args.spp_per_step)
+    nee_bytes_step = (cs.nee_vertices * NEE_B_VERTEX + cs.rays_shadow * NEE_B_RAY +
+                      cs.node_visits_nee * B_NODE + cs.tri_tests_nee * B_TRI)
+    nee_bytes_launch = nee_bytes_step / max(cs.launches_nee, 1)
+    avg_nee_s = nee_ms / 1e3 / max(nee_launches, 1)
+    achieved = nee_bytes_launch / avg_nee_s / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    tpv = profile_traffic()
+    traffic = None if tpv is None else tpv * cs.nee_vertices / max(cs.launches_nee, 1)
+    rc.close()
+    del rc
+    # end to end through the C ABI with host buffers: upload + BVH build +
+    # render + image read-back, per step
+    v, n, mi = sc.soup()
+    mats = sc.material_table()
+    h2d = v.nbytes + n.nbytes + mi.nbytes + 40 * mats.shape[0]
+    d2h = sc.width * sc.height * 3 * 4
+    e2e_steps = max(2, min(args.steps, 4))
+    e2e_rays, e2e_t = 0, 0.0
+    for i in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p2 = L.params_from_arrays(v, n, mi, mats, sc.width, sc.height, sc.eye, sc.look_at, sc.fov, 256, 8)
+        r2 = L.Renderer(p2, L.default_options(seed=1000 * rank + 7 + i, paths_in_flight=args.paths))
+        s2 = r2.render_progressive(args.spp_per_step)
+        img = r2.image()
+        r2.close()
+        dt = time.perf_counter() - t0
+        if i > 0:  # first one warms the allocator
+            e2e_rays += s2.rays
+            e2e_t += dt
+    e2e_val = sum_over_ranks(float(e2e_rays), ws) / max_over_ranks(e2e_t, ws) / 1e6
+    info = r.bvh_info()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cv, cdesc, ccores = cpu_sample(sc, spp=args.spp_per_step, budget_s=args.cpu_budget)
+        cpu = {"value": cv, "unit": "Mrays/s", "cores": ccores, "kind": "port", "sample": cdesc}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": sc.num_triangles, "width": sc.width,
+                       "height": sc.height, "spp_per_step": args.spp_per_step, "bounces": sc.num_bounces,
+                       "paths_in_flight": r.options.paths_in_flight or None,
+                       "l2": "working set > L2 (BVH+triangles+queues) and a 256 MB L2 flush before every step",
+                       "bvh": info, "sharding": "disjoint sample ranges per rank"},
+            "roofline": {"bound": "hbm", "kernel": "k_nee (emitter search + bounce)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic, "bytes_per_launch": nee_bytes_launch,
+                         "avg_launch_ms": avg_nee_s * 1e3,
+                         "per_unit": {"vertex_B": NEE_B_VERTEX, "shadow_ray_B": NEE_B_RAY, "node_B": B_NODE,
+                                      "tri_B": B_TRI},
+                         "counts_per_step": {"nee_vertices": cs.nee_vertices, "shadow_rays": cs.rays_shadow,
+                                             "node_visits": cs.node_visits_nee, "tri_tests": cs.tri_tests_nee}},
+            "stages_ms_per_step": {"trace": trace_ms / args.steps, "shade": shade_ms / args.steps,
+                                   "nee": nee_ms / args.steps, "other": other_ms / args.steps},
+            "rays_per_step": rays / args.steps,
+            "wall_s": wall,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "what": "Renderer create (H2D soup + GPU BVH build) + 16-spp render + FP32 image D2H"},
+            "clocks": clocks,
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp-per-step", type=int, default=16)
+    ap.add_argument("--paths", type=int, default=0, help="paths in flight (0 = library default)")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--ref-budget", type=float, default=6.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, ws, local = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_ours(args, rank, ws, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,595 @@
+// C ABI (include/lisa_gb.h) and renderer construction.
+//
+// Renderer construction replaces OptixWrapper (src/LiSA/src/optix_wrapper.cc):
+// the soup is uploaded once (create_mesh_handler :54-82), the BVH is built on
+// the GPU instead of optixAccelBuild (:92-145), the camera frame is the SDK
+// camera's UVW frame (src/sutil/Camera.cpp:34-45, set up in init_params
+// :434-442), and the launch state becomes the wavefront buffers.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "guide.cuh"
+#include "lisa_device.cuh"
+#include "lisa_internal.h"
+#include "wavefront.cuh"
+
+namespace lisa {
+
+Status configure_launch(Renderer& r);
+
+// ---- errors ---------------------------------------------------------------
+static thread_local std::string g_last_error;
+void set_last_error(const Status& s) { g_last_error = s.ok() ? std::string() : s.msg; }
+
+static int ret(const Status& s) {
+  set_last_error(s);
+  return s.code;
+}
+
+#define API_GUARD(...)                                     \
+  try {                                                     \
+    __VA_ARGS__                                             \
+  } catch (const std::bad_alloc&) {                         \
+    return ret(Status(LISA_ERR_OOM, "host allocation failed")); \
+  } catch (const std::exception& e) {                       \
+    return ret(Status(LISA_ERR_INVALID, e.what()));         \
+  } catch (...) {                                           \
+    return ret(Status(LISA_ERR_INVALID, "unknown error"));  \
+  }
+
+// ---- arena -----------------------------------------------------------------
+Status DeviceArena::alloc(void** p, size_t bytes, const char* what) {
+  bytes = std::max<size_t>(bytes, 16);
+  if (cap && used + bytes > cap)
+    return Status(LISA_ERR_OOM, std::string("allocation cap exceeded by ") + what);
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return Status(LISA_ERR_OOM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+  }
+  blocks.push_back(q);
+  used += bytes;
+  *p = q;
+  return Status();
+}
+
+void DeviceArena::release_all() {
+  for (void* p : blocks) cudaFree(p);
+  blocks.clear();
+  used = 0;
+}
+
+Renderer::~Renderer() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (auto e : ev_pool) cudaEventDestroy(e);
+  if (d_waves) cudaFree(d_waves);
+  guides.clear();
+  arena.release_all();
+  if (stream) cudaStreamDestroy(stream);
+}
+
+// ---- host vector math for the camera frame (Camera.cpp:34-45) ---------------
+namespace {
+struct H3 {
+  float x, y, z;
+};
+H3 hsub(H3 a, H3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+H3 hmul(H3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+float hdot(H3 a, H3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+H3 hcross(H3 a, H3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+H3 hnormalize(H3 v) { return hmul(v, 1.0f / std::sqrt(hdot(v, v))); }
+
+void camera_frame(const lisa_camera& c, uint32_t w, uint32_t h, float* eye, float* U, float* V, float* W) {
+  const H3 e{c.eye.x, c.eye.y, c.eye.z}, la{c.look_at.x, c.look_at.y, c.look_at.z}, up{0.0f, 1.0f, 0.0f};
+  const float aspect = (float)w / (float)h;
+  H3 Wv = hsub(la, e);  // not normalised: its length is the focal length
+  const float wlen = std::sqrt(hdot(Wv, Wv));
+  H3 Uv = hnormalize(hcross(Wv, up));
+  H3 Vv = hnormalize(hcross(Uv, Wv));
+  const float vlen = wlen * std::tan(0.5f * c.fov * 3.14159265358979323846f / 180.0f);
+  Vv = hmul(Vv, vlen);
+  const float ulen = vlen * aspect;
+  Uv = hmul(Uv, ulen);
+  eye[0] = e.x; eye[1] = e.y; eye[2] = e.z;
+  U[0] = Uv.x; U[1] = Uv.y; U[2] = Uv.z;
+  V[0] = Vv.x; V[1] = Vv.y; V[2] = Vv.z;
+  W[0] = Wv.x; W[1] = Wv.y; W[2] = Wv.z;
+}
+
+__global__ void k_pack_prims(const float* __restrict__ v, const float* __restrict__ nrm, const int32_t* __restrict__ mi,
+                             uint32_t n, float4* __restrict__ out) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const float* a = v + 9ull * p;
+    const float* b = nrm + 9ull * p;
+    float4* o = out + 5ull * p;
+    o[0] = make_float4(a[0], a[1], a[2], b[0]);
+    o[1] = make_float4(a[3], a[4], a[5], b[1]);
+    o[2] = make_float4(a[6], a[7], a[8], b[2]);
+    o[3] = make_float4(b[3], b[4], b[5], b[6]);
+    o[4] = make_float4(b[7], b[8], __int_as_float(mi[p]), 0.0f);
+  }
+}
+
+DevMaterial to_dev(const lisa_material& m) {
+  DevMaterial d;
+  std::memset(&d, 0, sizeof(d));
+  d.albedo[0] = m.diffuse_color.x;
+  d.albedo[1] = m.diffuse_color.y;
+  d.albedo[2] = m.diffuse_color.z;
+  d.roughness = m.roughness;
+  d.emission[0] = m.emission_color.x;
+  d.emission[1] = m.emission_color.y;
+  d.emission[2] = m.emission_color.z;
+  d.ior = m.n;
+  d.alpha = m.alpha;
+  // shader.cu:216 tests emit first, then alpha < 1 (:226)
+  d.cls = m.emit ? MAT_EMIT : (m.alpha < 1.0f ? MAT_DIELECTRIC : MAT_OPAQUE);
+  return d;
+}
+
+Status validate(const lisa_renderer_params& p) {
+  if (p.num_vertices < 0 || p.num_vertices % 3 != 0)
+    return Status::invalid("num_vertices must be a non-negative multiple of 3");
+  if (p.num_vertices > 0 && (!p.vertices || !p.normals || !p.mat_indices))
+    return Status::invalid("null soup pointer");
+  if (p.num_materials < 0 || (p.num_materials > 0 && !p.materials)) return Status::invalid("bad material table");
+  if (p.width == 0 || p.height == 0) return Status::invalid("width and height must be positive");
+  if ((uint64_t)p.width * p.height >= (1ull << 24)) return Status::invalid("at most 2^24 - 1 pixels per scene");
+  const uint32_t T = (uint32_t)(p.num_vertices / 3);
+  for (uint32_t i = 0; i < T; ++i)
+    if (p.mat_indices[i] < 0 || p.mat_indices[i] >= p.num_materials)
+      return Status::invalid("material index out of range at triangle " + std::to_string(i));
+  return Status();
+}
+}  // namespace
+
+Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
+  LISA_TRY(validate(p));
+  s.params = p;
+  s.output_image = p.output_image ? p.output_image : "";
+  s.params.output_image = nullptr;
+  s.params.vertices = nullptr;
+  s.params.normals = nullptr;
+  s.params.materials = nullptr;
+  s.params.mat_indices = nullptr;
+  s.num_prims = (uint32_t)(p.num_vertices / 3);
+  s.npix = p.width * p.height;
+  const uint32_t T = s.num_prims;
+  // upload the soup (72 B + 4 B per triangle) and pack the shading records
+  float *d_v = nullptr, *d_n = nullptr;
+  int32_t* d_m = nullptr;
+  if (T) {
+    LISA_CUDA(cudaMalloc(&d_v, sizeof(float) * 9ull * T));
+    LISA_CUDA(cudaMalloc(&d_n, sizeof(float) * 9ull * T));
+    LISA_CUDA(cudaMalloc(&d_m, sizeof(int32_t) * T));
+    LISA_CUDA(cudaMemcpyAsync(d_v, p.vertices, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice, r.stream));
+    LISA_CUDA(cudaMemcpyAsync(d_n, p.normals, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice, r.stream));
+    LISA_CUDA(cudaMemcpyAsync(d_m, p.mat_indices, sizeof(int32_t) * T, cudaMemcpyHostToDevice, r.stream));
+    LISA_TRY(r.arena.alloc((void**)&s.prims, sizeof(float4) * 5ull * T, "triangle records"));
+    k_pack_prims<<<r.sm_count * 8, 256, 0, r.stream>>>(d_v, d_n, d_m, T, s.prims);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      cudaFree(d_v);
+      cudaFree(d_n);
+      cudaFree(d_m);
+      return Status::cuda(e, "pack triangles");
+    }
+  }
+  Status st = build_bvh(d_v, T, r.stream, r.arena, &s.nodes, &s.tris, &s.bvh);
+  cudaStreamSynchronize(r.stream);
+  if (d_v) cudaFree(d_v);
+  if (d_n) cudaFree(d_n);
+  if (d_m) cudaFree(d_m);
+  LISA_TRY(st);
+  const float dx = s.bvh.bmax[0] - s.bvh.bmin[0], dy = s.bvh.bmax[1] - s.bvh.bmin[1],
+              dz = s.bvh.bmax[2] - s.bvh.bmin[2];
+  s.extent = std::sqrt(dx * dx + dy * dy + dz * dz);
+  if (!(s.extent > 0.0f) || !std::isfinite(s.extent)) s.extent = 1.0f;
+  // materials
+  std::vector<DevMaterial> dm(std::max(p.num_materials, 1));
+  for (int i = 0; i < p.num_materials; ++i) dm[i] = to_dev(p.materials[i]);
+  LISA_TRY(r.arena.alloc((void**)&s.mats, sizeof(DevMaterial) * dm.size(), "materials"));
+  LISA_CUDA(cudaMemcpyAsync(s.mats, dm.data(), sizeof(DevMaterial) * dm.size(), cudaMemcpyHostToDevice, r.stream));
+  // accumulation
+  LISA_TRY(r.arena.alloc((void**)&s.acc_sum, sizeof(float4) * s.npix, "accumulation"));
+  LISA_TRY(r.arena.alloc((void**)&s.acc_comp, sizeof(float4) * s.npix, "accumulation"));
+  LISA_TRY(r.arena.alloc((void**)&s.acc_sq, sizeof(double) * 3ull * s.npix, "variance"));
+  if (r.opts.accum_fp64) LISA_TRY(r.arena.alloc((void**)&s.acc_sum64, sizeof(double) * 3ull * s.npix, "fp64 mean"));
+  if (r.opts.rng == LISA_RNG_PER_PIXEL)
+    LISA_TRY(r.arena.alloc((void**)&s.pix_rng, sizeof(uint32_t) * s.npix, "pixel rng"));
+  LISA_CUDA(cudaMemsetAsync(s.acc_sum, 0, sizeof(float4) * s.npix, r.stream));
+  LISA_CUDA(cudaMemsetAsync(s.acc_comp, 0, sizeof(float4) * s.npix, r.stream));
+  LISA_CUDA(cudaMemsetAsync(s.acc_sq, 0, sizeof(double) * 3ull * s.npix, r.stream));
+  if (s.acc_sum64) LISA_CUDA(cudaMemsetAsync(s.acc_sum64, 0, sizeof(double) * 3ull * s.npix, r.stream));
+  camera_frame(p.camera, p.width, p.height, s.eye, s.U, s.V, s.W);
+  return Status();
+}
+
+SceneDev scene_dev(const Renderer& r, const SceneGpu& s) {
+  SceneDev d;
+  std::memset(&d, 0, sizeof(d));
+  d.nodes = s.nodes;
+  d.tris = s.tris;
+  d.prims = s.prims;
+  d.mats = s.mats;
+  d.num_prims = s.num_prims;
+  d.num_nodes = s.bvh.num_nodes;
+  d.num_mats = (uint32_t)std::max(s.params.num_materials, 0);
+  d.extent = s.extent;
+  d.width = s.params.width;
+  d.height = s.params.height;
+  d.num_bounces = s.params.num_bounces;
+  for (int k = 0; k < 3; ++k) {
+    d.eye[k] = s.eye[k];
+    d.U[k] = s.U[k];
+    d.V[k] = s.V[k];
+    d.W[k] = s.W[k];
+    d.bmin[k] = s.bvh.bmin[k];
+    d.bmax[k] = s.bvh.bmax[k];
+  }
+  d.lens_radius = r.opts.aperture;
+  const float ul = std::sqrt(s.U[0] * s.U[0] + s.U[1] * s.U[1] + s.U[2] * s.U[2]);
+  const float vl = std::sqrt(s.V[0] * s.V[0] + s.V[1] * s.V[1] + s.V[2] * s.V[2]);
+  const float wl = std::sqrt(s.W[0] * s.W[0] + s.W[1] * s.W[1] + s.W[2] * s.W[2]);
+  for (int k = 0; k < 3; ++k) {
+    d.unitU[k] = ul > 0 ? s.U[k] / ul : 0.0f;
+    d.unitV[k] = vl > 0 ? s.V[k] / vl : 0.0f;
+    d.unitW[k] = wl > 0 ? s.W[k] / wl : 0.0f;
+  }
+  d.focal_distance = r.opts.focal_distance > 0.0f ? r.opts.focal_distance : wl;
+  d.acc_sum = s.acc_sum;
+  d.acc_comp = s.acc_comp;
+  d.acc_sq = s.acc_sq;
+  d.acc_sum64 = s.acc_sum64;
+  d.pix_rng = s.pix_rng;
+  d.guide = s.guide;
+  return d;
+}
+
+Status renderer_create(const lisa_renderer_params* scenes, int n, const lisa_options* opts, Renderer** out) {
+  if (!scenes || n <= 0 || !out) return Status::invalid("no scenes");
+  if (n > 255) return Status::invalid("at most 255 scenes per renderer");
+  std::unique_ptr<Renderer> r(new Renderer());
+  lisa_options_default(&r->opts);
+  if (opts) {
+    if (opts->struct_size != sizeof(lisa_options)) return Status::invalid("lisa_options.struct_size mismatch");
+    r->opts = *opts;
+  }
+  if (r->opts.mode > LISA_MODE_GUIDED) return Status::invalid("unknown mode");
+  if (r->opts.rng > LISA_RNG_PER_PIXEL) return Status::invalid("unknown rng mode");
+  r->arena.cap = r->opts.alloc_cap_bytes;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return Status(LISA_ERR_UNSUPPORTED, "no CUDA device");
+  }
+  LISA_CUDA(cudaGetDevice(&r->device));
+  cudaDeviceProp prop;
+  LISA_CUDA(cudaGetDeviceProperties(&prop, r->device));
+  if (prop.major < 10) return Status(LISA_ERR_UNSUPPORTED, "needs a Blackwell (sm_10x) GPU");
+  r->sm_count = prop.multiProcessorCount;
+  LISA_CUDA(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
+  r->scenes.resize(n);
+  uint64_t total_paths = 0;
+  for (int i = 0; i < n; ++i) {
+    LISA_TRY(create_scene(*r, scenes[i], r->scenes[i]));
+    total_paths += (uint64_t)r->scenes[i].npix * std::max<uint32_t>(scenes[i].num_samples, 1);
+  }
+  // wavefront capacity
+  uint64_t W = r->opts.paths_in_flight ? r->opts.paths_in_flight : (1ull << 22);
+  W = std::min<uint64_t>(W, std::max<uint64_t>(total_paths, 1));
+  W = std::max<uint64_t>(W, 32);
+  if (W > (1ull << 30)) return Status::invalid("paths_in_flight too large");
+  r->capacity = (uint32_t)W;
+  for (int k = 0; k < 2; ++k) {
+    LISA_TRY(r->arena.alloc((void**)&r->ro[k], sizeof(float4) * W, "ray queue"));
+    LISA_TRY(r->arena.alloc((void**)&r->rd[k], sizeof(float4) * W, "ray queue"));
+  }
+  LISA_TRY(r->arena.alloc((void**)&r->hit, sizeof(int2) * W, "hit queue"));
+  LISA_TRY(r->arena.alloc((void**)&r->ps_att, sizeof(float4) * W, "path state"));
+  LISA_TRY(r->arena.alloc((void**)&r->ps_col, sizeof(float4) * W, "path state"));
+  LISA_TRY(r->arena.alloc((void**)&r->ps_rng, sizeof(uint32_t) * W, "path state"));
+  LISA_TRY(r->arena.alloc((void**)&r->nee_a, sizeof(float4) * W, "emitter queue"));
+  LISA_TRY(r->arena.alloc((void**)&r->nee_b, sizeof(float4) * W, "emitter queue"));
+  LISA_TRY(r->arena.alloc((void**)&r->nee_c, sizeof(float4) * W, "emitter queue"));
+  LISA_TRY(r->arena.alloc((void**)&r->ctrl, sizeof(WaveCtrl), "control block"));
+  LISA_CUDA(cudaMemsetAsync(r->ctrl, 0, sizeof(WaveCtrl), r->stream));
+  if (r->opts.mode == LISA_MODE_GUIDED) LISA_TRY(guide_renderer_init(*r));
+  std::vector<SceneDev> sd(n);
+  for (int i = 0; i < n; ++i) sd[i] = scene_dev(*r, r->scenes[i]);
+  LISA_TRY(r->arena.alloc((void**)&r->d_scenes, sizeof(SceneDev) * n, "scene table"));
+  LISA_CUDA(cudaMemcpyAsync(r->d_scenes, sd.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice, r->stream));
+  LISA_TRY(configure_launch(*r));
+  LISA_CUDA(cudaStreamSynchronize(r->stream));
+  *out = r.release();
+  return Status();
+}
+
+// ---- PPM (sutil.cpp:97-117, 523-553) ------------------------------------------
+Status write_ppm_rgb8_flipped(const char* path, const uint8_t* rgb8, uint32_t w, uint32_t h) {
+  if (!path || !rgb8 || w < 1 || h < 1) return Status::invalid("savePPM: Image is ill-formed. Not saving");
+  const std::string fn(path);
+  if (fn.size() < 5) return Status::invalid("saveImage(): Failed to determine filename extension");
+  const std::string ext = fn.substr(fn.size() - 3);
+  if (ext != "ppm" && ext != "PPM") return Status::invalid("saveImage(): only .ppm output is supported");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return Status::io("savePPM: Could not open file for writing: " + fn);
+  std::fprintf(f, "P6\n%u %u\n255\n", w, h);
+  const size_t n = 3ull * w * h;
+  const size_t wrote = std::fwrite(rgb8, 1, n, f);
+  std::fclose(f);
+  if (wrote != n) return Status::io("savePPM: short write");
+  return Status();
+}
+
+Status write_ppm_rgba8(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h) {
+  if (!rgba8 || w < 1 || h < 1) return Status::invalid("savePPM: Image is ill-formed. Not saving");
+  std::vector<uint8_t> pix(3ull * w * h);
+  for (int64_t j = (int64_t)h - 1; j >= 0; --j)
+    for (uint32_t i = 0; i < w; ++i) {
+      const size_t dst = 3ull * w * (h - j - 1) + 3ull * i;
+      const size_t src = 4ull * w * j + 4ull * i;
+      pix[dst] = rgba8[src];
+      pix[dst + 1] = rgba8[src + 1];
+      pix[dst + 2] = rgba8[src + 2];
+    }
+  return write_ppm_rgb8_flipped(path, pix.data(), w, h);
+}
+
+}  // namespace lisa
+
+// ===========================================================================
+// extern "C"
+using namespace lisa;
+
+struct lisa_scene {
+  Scene s;
+};
+struct lisa_renderer {
+  Renderer* r;
+};
+
+extern "C" {
+
+const char* lisa_last_error(void) { return g_last_error.c_str(); }
+
+const char* lisa_version(void) { return "lisa_gb300 1.0 (sm_103a)"; }
+
+int lisa_device_info(int* sm_count, int* cc_major, int* cc_minor) {
+  API_GUARD({
+    int dev = 0, n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+      cudaGetLastError();
+      return ret(Status(LISA_ERR_UNSUPPORTED, "no CUDA device"));
+    }
+    cudaDeviceProp p;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess || (e = cudaGetDeviceProperties(&p, dev)) != cudaSuccess)
+      return ret(Status::cuda(e, "device query"));
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+    return ret(Status());
+  })
+}
+
+int lisa_scene_parse(const char* rto_path, lisa_scene** out) {
+  API_GUARD({
+    if (!rto_path || !out) return ret(Status::invalid("null argument"));
+    std::unique_ptr<lisa_scene> sc(new lisa_scene());
+    Status s = parse_scene_file(rto_path, sc->s);
+    if (!s.ok()) return ret(s);
+    *out = sc.release();
+    return ret(Status());
+  })
+}
+
+int lisa_scene_parse_string(const char* text, size_t len, const char* base_dir, lisa_scene** out) {
+  API_GUARD({
+    if (!text || !out) return ret(Status::invalid("null argument"));
+    std::unique_ptr<lisa_scene> sc(new lisa_scene());
+    Status s = parse_scene_text(std::string(text, len), base_dir ? base_dir : "", sc->s);
+    if (!s.ok()) return ret(s);
+    *out = sc.release();
+    return ret(Status());
+  })
+}
+
+int lisa_scene_params(const lisa_scene* scene, lisa_renderer_params* out) {
+  API_GUARD({
+    if (!scene || !out) return ret(Status::invalid("null argument"));
+    scene_fill_params(scene->s, out);
+    return ret(Status());
+  })
+}
+
+void lisa_scene_destroy(lisa_scene* scene) { delete scene; }
+
+int lisa_scene_create_empty(lisa_scene** out) {
+  API_GUARD({
+    if (!out) return ret(Status::invalid("null argument"));
+    *out = new lisa_scene();
+    return ret(Status());
+  })
+}
+
+int lisa_scene_append_obj(lisa_scene* scene, const char* obj_path, int32_t mat_idx) {
+  API_GUARD({
+    if (!scene || !obj_path) return ret(Status::invalid("null argument"));
+    return ret(obj_append(scene->s, obj_path, mat_idx));
+  })
+}
+
+void lisa_options_default(lisa_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->struct_size = sizeof(lisa_options);
+  o->mode = LISA_MODE_COMPAT;
+  o->rng = LISA_RNG_PER_SAMPLE;
+  o->use_graph = 1;
+  o->guide_bsdf_fraction = 0.5f;
+  o->guide_lr = 1e-2f;
+  o->guide_train_batch = 1u << 16;
+}
+
+int lisa_renderer_create(const lisa_renderer_params* params, const lisa_options* opts, lisa_renderer** out) {
+  return lisa_renderer_create_batch(params, 1, opts, out);
+}
+
+int lisa_renderer_create_batch(const lisa_renderer_params* scenes, int32_t n, const lisa_options* opts,
+                               lisa_renderer** out) {
+  API_GUARD({
+    if (!out) return ret(Status::invalid("null argument"));
+    Renderer* r = nullptr;
+    Status s = renderer_create(scenes, n, opts, &r);
+    if (!s.ok()) return ret(s);
+    *out = new lisa_renderer{r};
+    return ret(Status());
+  })
+}
+
+void lisa_renderer_destroy(lisa_renderer* r) {
+  if (!r) return;
+  delete r->r;
+  delete r;
+}
+
+int lisa_render(lisa_renderer* r, lisa_render_stats* stats) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    return ret(renderer_render(*r->r, 0, false, stats));
+  })
+}
+
+int lisa_render_progressive(lisa_renderer* r, uint32_t spp, lisa_render_stats* stats) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    if (spp == 0) return ret(Status::invalid("spp must be positive"));
+    return ret(renderer_render(*r->r, spp, true, stats));
+  })
+}
+
+int lisa_reset_accumulation(lisa_renderer* r) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    return ret(renderer_reset(*r->r));
+  })
+}
+
+int lisa_get_image(lisa_renderer* r, int32_t scene, float* rgb32, uint8_t* rgba8, double* var, double* mean64) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    return ret(renderer_get_image(*r->r, scene, rgb32, rgba8, var, mean64));
+  })
+}
+
+int lisa_get_ppm_rgb8(lisa_renderer* r, int32_t scene, uint8_t* rgb8) {
+  API_GUARD({
+    if (!r || !rgb8) return ret(Status::invalid("null argument"));
+    return ret(renderer_get_ppm(*r->r, scene, rgb8));
+  })
+}
+
+int lisa_save_image(lisa_renderer* r, int32_t scene, const char* path) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    Renderer& R = *r->r;
+    if (scene < 0 || scene >= (int)R.scenes.size()) return ret(Status::invalid("scene index out of range"));
+    SceneGpu& s = R.scenes[scene];
+    std::vector<uint8_t> rgb(3ull * s.npix);
+    Status st = renderer_get_ppm(R, scene, rgb.data());
+    if (!st.ok()) return ret(st);
+    const std::string p = path ? std::string(path) : s.output_image;
+    return ret(write_ppm_rgb8_flipped(p.c_str(), rgb.data(), s.params.width, s.params.height));
+  })
+}
+
+int lisa_write_ppm(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height) {
+  API_GUARD({ return ret(write_ppm_rgba8(path, rgba8, width, height)); })
+}
+
+int lisa_trace_closest(lisa_renderer* r, const float* rays, uint32_t n, int32_t* prim, float* t) {
+  API_GUARD({
+    if (!r || (n && (!rays || !prim || !t))) return ret(Status::invalid("null argument"));
+    if (n == 0) return ret(Status());
+    Renderer& R = *r->r;
+    float* d_r = nullptr;
+    int32_t* d_p = nullptr;
+    float* d_t = nullptr;
+    Status s;
+    auto run = [&]() -> Status {
+      LISA_CUDA(cudaMalloc(&d_r, sizeof(float) * 8ull * n));
+      LISA_CUDA(cudaMalloc(&d_p, sizeof(int32_t) * n));
+      LISA_CUDA(cudaMalloc(&d_t, sizeof(float) * n));
+      LISA_CUDA(cudaMemcpyAsync(d_r, rays, sizeof(float) * 8ull * n, cudaMemcpyHostToDevice, R.stream));
+      LISA_TRY(trace_rays(R, d_r, n, d_p, d_t, R.stream, false));
+      LISA_CUDA(cudaMemcpyAsync(prim, d_p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, R.stream));
+      LISA_CUDA(cudaMemcpyAsync(t, d_t, sizeof(float) * n, cudaMemcpyDeviceToHost, R.stream));
+      LISA_CUDA(cudaStreamSynchronize(R.stream));
+      return Status();
+    };
+    s = run();
+    if (d_r) cudaFree(d_r);
+    if (d_p) cudaFree(d_p);
+    if (d_t) cudaFree(d_t);
+    return ret(s);
+  })
+}
+
+int lisa_trace_closest_device(lisa_renderer* r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t,
+                              void* stream) {
+  API_GUARD({
+    if (!r || (n && (!d_rays || !d_prim || !d_t))) return ret(Status::invalid("null argument"));
+    Renderer& R = *r->r;
+    return ret(trace_rays(R, d_rays, n, d_prim, d_t, stream ? (cudaStream_t)stream : R.stream, false));
+  })
+}
+
+int lisa_trace_brute_device(lisa_renderer* r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t,
+                            void* stream) {
+  API_GUARD({
+    if (!r || (n && (!d_rays || !d_prim || !d_t))) return ret(Status::invalid("null argument"));
+    Renderer& R = *r->r;
+    return ret(trace_rays(R, d_rays, n, d_prim, d_t, stream ? (cudaStream_t)stream : R.stream, true));
+  })
+}
+
+int lisa_trace_count(lisa_renderer* r, const float* rays, uint32_t n, uint64_t* node_visits, uint64_t* tri_tests) {
+  API_GUARD({
+    if (!r || !node_visits || !tri_tests || (n && !rays)) return ret(Status::invalid("null argument"));
+    Renderer& R = *r->r;
+    float* d_r = nullptr;
+    auto run = [&]() -> Status {
+      LISA_CUDA(cudaMalloc(&d_r, sizeof(float) * 8ull * std::max<uint32_t>(n, 1)));
+      if (n) LISA_CUDA(cudaMemcpyAsync(d_r, rays, sizeof(float) * 8ull * n, cudaMemcpyHostToDevice, R.stream));
+      return trace_count(R, d_r, n, node_visits, tri_tests);
+    };
+    Status s = run();
+    if (d_r) cudaFree(d_r);
+    return ret(s);
+  })
+}
+
+int lisa_bvh_info(lisa_renderer* r, int32_t scene, uint32_t* nodes, uint32_t* tri_slots, uint32_t* depth,
+                  double* build_ms) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    Renderer& R = *r->r;
+    if (scene < 0 || scene >= (int)R.scenes.size()) return ret(Status::invalid("scene index out of range"));
+    const BvhBuildResult& b = R.scenes[scene].bvh;
+    if (nodes) *nodes = b.num_nodes;
+    if (tri_slots) *tri_slots = b.num_tri_slots;
+    if (depth) *depth = b.depth;
+    if (build_ms) *build_ms = b.build_ms;
+    return ret(Status());
+  })
+}
+
+}  // extern "C"

@@ -1,0 +1,634 @@
+// GPU BVH construction for the triangle soup.
+//
+// Replaces the closed optixAccelBuild call of the reference
+// (src/LiSA/src/optix_wrapper.cc:92-145).  Pipeline, all on the device:
+//   1. per-triangle AABB and centroid, scene and centroid bounds
+//   2. 30-bit Morton code of each centroid
+//   3. stable LSD radix sort of (code, triangle) pairs: 4 passes of 8 bits,
+//      tile histograms -> exclusive scan -> stable scatter (warp match-any
+//      ranking), written here without a sort library
+//   4. binary radix tree over the sorted codes (Karras, "Maximizing
+//      Parallelism in the Construction of BVHs, Octrees, and k-d Trees",
+//      HPG 2012), equal codes ordered by index
+//   5. bottom-up AABBs with one atomic arrival counter per node
+//   6. collapse into 8-wide nodes, level by level: each node adopts up to 8
+//      descendants by repeatedly opening the child of largest surface area
+//      (subtrees of <= 3 triangles become leaves), then stores its child
+//      boxes quantised to 8 bits against a per-axis power-of-two grid,
+//      rounded outward (compressed layout in the style of Ylitie, Karras,
+//      Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed
+//      Wide BVHs", HPG 2017).  Leaf triangles are copied into leaf order.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lisa_device.cuh"
+#include "lisa_internal.h"
+
+namespace lisa {
+namespace {
+
+constexpr uint32_t LEAF_BIT = 0x80000000u;
+
+__device__ __forceinline__ int f2ord(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__host__ __device__ __forceinline__ float ord2f(int i) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff);
+#else
+  const int j = i >= 0 ? i : i ^ 0x7fffffff;
+  float f;
+  std::memcpy(&f, &j, 4);
+  return f;
+#endif
+}
+
+// bounds[0..2] = min scene xyz, [3..5] = max scene xyz, [6..8] min centroid,
+// [9..11] max centroid, as order-preserving ints.
+__global__ void k_prim_bounds(const float* __restrict__ v, uint32_t n, float4* __restrict__ lo,
+                              float4* __restrict__ hi, int* bounds) {
+  float mn[6], mx[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    mn[k] = __int_as_float(0x7f800000);
+    mx[k] = -__int_as_float(0x7f800000);
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* t = v + 9ull * i;
+    float a[3], b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      a[k] = fminf(fminf(t[k], t[3 + k]), t[6 + k]);
+      b[k] = fmaxf(fmaxf(t[k], t[3 + k]), t[6 + k]);
+      const float c = 0.5f * (a[k] + b[k]);
+      mn[k] = fminf(mn[k], a[k]);
+      mx[k] = fmaxf(mx[k], b[k]);
+      mn[3 + k] = fminf(mn[3 + k], c);
+      mx[3 + k] = fmaxf(mx[3 + k], c);
+    }
+    lo[i] = make_float4(a[0], a[1], a[2], 0.0f);
+    hi[i] = make_float4(b[0], b[1], b[2], 0.0f);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      atomicMin(&bounds[k], f2ord(mn[k]));
+      atomicMax(&bounds[3 + k], f2ord(mx[k]));
+      atomicMin(&bounds[6 + k], f2ord(mn[3 + k]));
+      atomicMax(&bounds[9 + k], f2ord(mx[3 + k]));
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t expand10(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+__global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, uint32_t n,
+                         const int* __restrict__ bounds, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = lo[i], b = hi[i];
+  const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+  uint32_t q[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float cmin = ord2f(bounds[6 + k]), cmax = ord2f(bounds[9 + k]);
+    const float ext = cmax - cmin;
+    float u = ext > 0.0f ? (c[k] - cmin) / ext : 0.5f;
+    u = fminf(fmaxf(u, 0.0f), 1.0f);
+    q[k] = min((uint32_t)(u * 1024.0f), 1023u);
+  }
+  keys[i] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+  vals[i] = i;
+}
+
+// ---- radix sort -----------------------------------------------------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ROUNDS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ROUNDS;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift,
+                                                       uint32_t* __restrict__ hist, uint32_t num_tiles) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+  for (int k = 0; k < RS_ROUNDS; ++k) {
+    const uint64_t idx = base + (uint64_t)k * RS_THREADS + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(uint64_t)threadIdx.x * num_tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                          uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                          uint32_t n, int shift, const uint32_t* __restrict__ offs,
+                                                          uint32_t num_tiles) {
+  __shared__ uint32_t s_base[256];
+  __shared__ uint32_t s_run[256];
+  __shared__ uint32_t s_wc[RS_THREADS / 32][256];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  s_base[tid] = offs[(uint64_t)tid * num_tiles + blockIdx.x];
+  s_run[tid] = 0;
+  const uint64_t base = (uint64_t)blockIdx.x * RS_TILE;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int r = 0; r < RS_ROUNDS; ++r) {
+#pragma unroll
+    for (int w = 0; w < RS_THREADS / 32; ++w) s_wc[w][tid] = 0;
+    __syncthreads();
+    const uint64_t idx = base + (uint64_t)r * RS_THREADS + tid;
+    const bool valid = idx < n;
+    const uint32_t key = valid ? kin[idx] : 0u;
+    const uint32_t d = valid ? ((key >> shift) & 255u) : 256u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t rank = __popc(peers & lt);
+    if (valid && rank == 0) s_wc[warp][d] = __popc(peers);
+    __syncthreads();
+    uint32_t run = s_run[tid];
+#pragma unroll
+    for (int w = 0; w < RS_THREADS / 32; ++w) {
+      const uint32_t c = s_wc[w][tid];
+      s_wc[w][tid] = run;
+      run += c;
+    }
+    s_run[tid] = run;
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = s_base[d] + s_wc[warp][d] + rank;
+      kout[pos] = key;
+      vout[pos] = vin[idx];
+    }
+    __syncthreads();
+  }
+}
+
+// ---- exclusive scan (in place) --------------------------------------------
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t ws[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    uint32_t s = lane < nw ? ws[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) ws[lane] = s;
+  }
+  __syncthreads();
+  const uint32_t before = (warp > 0 ? ws[warp - 1] : 0u) + x - v;
+  if (total) *total = ws[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_blocks(uint32_t* data, uint64_t m, uint32_t* sums) {
+  const uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    v[k] = (base + k < m) ? data[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t total;
+  uint32_t run = block_exclusive(s, &total);
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    if (base + k < m) data[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* sums, uint32_t nb) {
+  uint32_t carry = 0;
+  for (uint32_t c0 = 0; c0 < nb; c0 += SCAN_CHUNK) {
+    const uint32_t base = c0 + threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+      v[k] = (base + k < nb) ? sums[base + k] : 0u;
+      s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = carry + block_exclusive(s, &total);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+      if (base + k < nb) sums[base + k] = run;
+      run += v[k];
+    }
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_add(uint32_t* data, uint64_t m, const uint32_t* sums) {
+  const uint64_t base = (uint64_t)blockIdx.x * SCAN_CHUNK + (uint64_t)threadIdx.x * SCAN_ITEMS;
+  const uint32_t add = sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k)
+    if (base + k < m) data[base + k] += add;
+}
+
+// ---- Karras radix tree ------------------------------------------------------
+__device__ __forceinline__ int kdelta(const uint32_t* keys, int64_t n, int64_t i, int64_t j) {
+  if (j < 0 || j >= n) return -1;
+  const uint32_t a = keys[i], b = keys[j];
+  if (a == b) return 32 + __clz((uint32_t)(i ^ j));
+  return __clz(a ^ b);
+}
+
+__global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ left,
+                         uint32_t* __restrict__ right, uint32_t* __restrict__ first, uint32_t* __restrict__ last,
+                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)n - 1) return;
+  const int64_t N = n;
+  const int d = (kdelta(keys, N, i, i + 1) - kdelta(keys, N, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = kdelta(keys, N, i, i - d);
+  int64_t lmax = 2;
+  while (kdelta(keys, N, i, i + lmax * d) > dmin) lmax <<= 1;
+  int64_t l = 0;
+  for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+    if (kdelta(keys, N, i, i + (l + t) * d) > dmin) l += t;
+  const int64_t j = i + l * d;
+  const int dnode = kdelta(keys, N, i, j);
+  int64_t s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (kdelta(keys, N, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+  const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+  const uint32_t lc = (lo == gamma) ? (LEAF_BIT | (uint32_t)gamma) : (uint32_t)gamma;
+  const uint32_t rc = (hi == gamma + 1) ? (LEAF_BIT | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
+  left[i] = lc;
+  right[i] = rc;
+  first[i] = (uint32_t)lo;
+  last[i] = (uint32_t)hi;
+  if (lc & LEAF_BIT) parent_leaf[lc & ~LEAF_BIT] = (uint32_t)i; else parent_int[lc] = (uint32_t)i;
+  if (rc & LEAF_BIT) parent_leaf[rc & ~LEAF_BIT] = (uint32_t)i; else parent_int[rc] = (uint32_t)i;
+  if (i == 0) parent_int[0] = 0xffffffffu;
+}
+
+__device__ __forceinline__ void node_box(uint32_t c, const uint32_t* vals, const float4* plo, const float4* phi,
+                                         const float4* ilo, const float4* ihi, float4& lo, float4& hi) {
+  if (c & LEAF_BIT) {
+    const uint32_t p = vals[c & ~LEAF_BIT];
+    lo = plo[p];
+    hi = phi[p];
+  } else {
+    lo = __ldcg(ilo + c);
+    hi = __ldcg(ihi + c);
+  }
+}
+
+__global__ void k_bottom_up(uint32_t n, const uint32_t* __restrict__ vals, const float4* __restrict__ plo,
+                            const float4* __restrict__ phi, const uint32_t* __restrict__ parent_leaf,
+                            const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ left,
+                            const uint32_t* __restrict__ right, float4* ilo, float4* ihi, uint32_t* flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || n < 2) return;
+  uint32_t p = parent_leaf[i];
+  while (p != 0xffffffffu) {
+    __threadfence();
+    if (atomicAdd(&flags[p], 1u) == 0u) return;
+    __threadfence();
+    float4 a0, a1, b0, b1;
+    node_box(left[p], vals, plo, phi, ilo, ihi, a0, a1);
+    node_box(right[p], vals, plo, phi, ilo, ihi, b0, b1);
+    __stcg(ilo + p, make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 0.0f));
+    __stcg(ihi + p, make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f));
+    p = parent_int[p];
+  }
+}
+
+// ---- collapse to 8-wide compressed nodes -------------------------------------
+struct CollapseArgs {
+  uint32_t n;
+  const uint32_t* vals;
+  const float4* plo;
+  const float4* phi;
+  const float4* ilo;
+  const float4* ihi;
+  const uint32_t* left;
+  const uint32_t* right;
+  const uint32_t* first;
+  const uint32_t* last;
+  const float* verts;
+  uint4* nodes;
+  float4* tris;
+  uint32_t* counters;  // [0] nodes, [1] tri slots, [2] next work count
+};
+
+__device__ __forceinline__ uint32_t sub_count(const CollapseArgs& a, uint32_t c) {
+  return (c & LEAF_BIT) ? 1u : (a.last[c] - a.first[c] + 1u);
+}
+__device__ __forceinline__ uint32_t sub_first(const CollapseArgs& a, uint32_t c) {
+  return (c & LEAF_BIT) ? (c & ~LEAF_BIT) : a.first[c];
+}
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+  const float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
+  return x * y + y * z + z * x;
+}
+
+// Smallest e with 255 * 2^e >= ext, clamped to the normal float range.
+__device__ int grid_exponent(double ext) {
+  if (!(ext > 0.0)) return -126;
+  int e;
+  frexp(ext / 255.0, &e);  // ext/255 = m * 2^e, m in [0.5, 1)
+  while (ldexp(255.0, e - 1) >= ext && e > -126) --e;
+  while (ldexp(255.0, e) < ext) ++e;
+  return max(-126, min(127, e));
+}
+
+__global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ work, uint32_t nwork, uint2* __restrict__ next) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwork) return;
+  const uint32_t dst = work[w].x, src = work[w].y;
+  uint32_t cand[8];
+  int nc;
+  if (!(src & LEAF_BIT) && sub_count(a, src) > 3u) {
+    cand[0] = a.left[src];
+    cand[1] = a.right[src];
+    nc = 2;
+  } else {
+    cand[0] = src;
+    nc = 1;
+  }
+  float4 clo[8], chi[8];
+  for (int k = 0; k < nc; ++k) node_box(cand[k], a.vals, a.plo, a.phi, a.ilo, a.ihi, clo[k], chi[k]);
+  while (nc < 8) {
+    int best = -1;
+    float best_area = -1.0f;
+    for (int k = 0; k < nc; ++k) {
+      if ((cand[k] & LEAF_BIT) || sub_count(a, cand[k]) <= 3u) continue;
+      const float ar = half_area(clo[k], chi[k]);
+      if (ar > best_area) {
+        best_area = ar;
+        best = k;
+      }
+    }
+    if (best < 0) break;
+    const uint32_t c = cand[best];
+    cand[best] = a.left[c];
+    cand[nc] = a.right[c];
+    node_box(cand[best], a.vals, a.plo, a.phi, a.ilo, a.ihi, clo[best], chi[best]);
+    node_box(cand[nc], a.vals, a.plo, a.phi, a.ilo, a.ihi, clo[nc], chi[nc]);
+    ++nc;
+  }
+  uint32_t num_int = 0, num_tri = 0;
+  for (int k = 0; k < nc; ++k) {
+    const uint32_t cnt = sub_count(a, cand[k]);
+    if (cnt > 3u) ++num_int; else num_tri += cnt;
+  }
+  const uint32_t child_base = num_int ? atomicAdd(&a.counters[0], num_int) : 0u;
+  const uint32_t tri_base = num_tri ? atomicAdd(&a.counters[1], num_tri) : 0u;
+  // node frame
+  float4 nlo = clo[0], nhi = chi[0];
+  for (int k = 1; k < nc; ++k) {
+    nlo.x = fminf(nlo.x, clo[k].x);
+    nlo.y = fminf(nlo.y, clo[k].y);
+    nlo.z = fminf(nlo.z, clo[k].z);
+    nhi.x = fmaxf(nhi.x, chi[k].x);
+    nhi.y = fmaxf(nhi.y, chi[k].y);
+    nhi.z = fmaxf(nhi.z, chi[k].z);
+  }
+  const float p[3] = {nlo.x, nlo.y, nlo.z};
+  const float ph[3] = {nhi.x, nhi.y, nhi.z};
+  int e[3];
+  for (int ax = 0; ax < 3; ++ax) e[ax] = grid_exponent((double)ph[ax] - (double)p[ax]);
+  uint8_t qlo[3][8], qhi[3][8], meta[8];
+  uint32_t imask = 0, rank = 0, toff = 0;
+  for (int k = 0; k < 8; ++k) {
+    meta[k] = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+      qlo[ax][k] = 0;
+      qhi[ax][k] = 0;
+    }
+  }
+  for (int k = 0; k < nc; ++k) {
+    const float lo3[3] = {clo[k].x, clo[k].y, clo[k].z};
+    const float hi3[3] = {chi[k].x, chi[k].y, chi[k].z};
+    for (int ax = 0; ax < 3; ++ax) {
+      const double sc = ldexp(1.0, e[ax]);
+      double ql = floor(((double)lo3[ax] - (double)p[ax]) / sc);
+      double qh = ceil(((double)hi3[ax] - (double)p[ax]) / sc);
+      ql = fmin(fmax(ql, 0.0), 255.0);
+      qh = fmin(fmax(qh, 0.0), 255.0);
+      while (ql > 0.0 && (double)p[ax] + ql * sc > (double)lo3[ax]) ql -= 1.0;
+      while (qh < 255.0 && (double)p[ax] + qh * sc < (double)hi3[ax]) qh += 1.0;
+      qlo[ax][k] = (uint8_t)ql;
+      qhi[ax][k] = (uint8_t)qh;
+    }
+    const uint32_t cnt = sub_count(a, cand[k]);
+    if (cnt > 3u) {
+      imask |= 1u << k;
+      meta[k] = (uint8_t)rank;
+      const uint32_t slot = atomicAdd(&a.counters[2], 1u);
+      next[slot] = make_uint2(child_base + rank, cand[k]);
+      ++rank;
+    } else {
+      meta[k] = (uint8_t)((cnt << 5) | toff);
+      const uint32_t f0 = sub_first(a, cand[k]);
+      for (uint32_t q = 0; q < cnt; ++q) {
+        const uint32_t prim = a.vals[f0 + q];
+        const float* t = a.verts + 9ull * prim;
+        float4* o = a.tris + 3ull * (tri_base + toff + q);
+        o[0] = make_float4(t[0], t[1], t[2], __int_as_float((int)prim));
+        o[1] = make_float4(t[3], t[4], t[5], 0.0f);
+        o[2] = make_float4(t[6], t[7], t[8], 0.0f);
+      }
+      toff += cnt;
+    }
+  }
+  auto pack4 = [](const uint8_t* b) {
+    return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+  };
+  uint4* np = a.nodes + 5ull * dst;
+  np[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]),
+                     (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) |
+                         (imask << 24));
+  np[1] = make_uint4(child_base, tri_base, pack4(meta), pack4(meta + 4));
+  np[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
+  np[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
+  np[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+}
+
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+Status device_exclusive_scan(uint32_t* d, uint64_t m, uint32_t* tmp, cudaStream_t s) {
+  const uint32_t nb = cdiv(m, SCAN_CHUNK);
+  k_scan_blocks<<<nb, SCAN_THREADS, 0, s>>>(d, m, tmp);
+  k_scan_single<<<1, SCAN_THREADS, 0, s>>>(tmp, nb);
+  k_scan_add<<<nb, SCAN_THREADS, 0, s>>>(d, m, tmp);
+  LISA_CUDA(cudaGetLastError());
+  return Status();
+}
+
+// Sorts (keys, vals) by the low 32 bits of keys; stable.  Result in keys/vals.
+Status device_radix_sort(uint32_t* keys, uint32_t* vals, uint32_t* keys2, uint32_t* vals2, uint32_t n,
+                         uint32_t* hist, uint32_t* scan_tmp, int bits, cudaStream_t s) {
+  const uint32_t tiles = cdiv(n, RS_TILE);
+  uint32_t *ki = keys, *vi = vals, *ko = keys2, *vo = vals2;
+  for (int shift = 0; shift < bits; shift += 8) {
+    k_rs_hist<<<tiles, RS_THREADS, 0, s>>>(ki, n, shift, hist, tiles);
+    LISA_TRY(device_exclusive_scan(hist, 256ull * tiles, scan_tmp, s));
+    k_rs_scatter<<<tiles, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+    LISA_CUDA(cudaGetLastError());
+    std::swap(ki, ko);
+    std::swap(vi, vo);
+  }
+  if (ki != keys) {
+    LISA_CUDA(cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+    LISA_CUDA(cudaMemcpyAsync(vals, vi, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  return Status();
+}
+
+namespace {
+struct TmpBufs {
+  std::vector<void*> ptrs;
+  ~TmpBufs() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <class T>
+  Status get(T** p, size_t count) {
+    void* q = nullptr;
+    LISA_CUDA(cudaMalloc(&q, std::max<size_t>(count * sizeof(T), 16)));
+    ptrs.push_back(q);
+    *p = (T*)q;
+    return Status();
+  }
+};
+}  // namespace
+
+Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, DeviceArena& arena, uint4** d_nodes,
+                 float4** d_tris, BvhBuildResult* info) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (n == 0) {
+    *d_nodes = nullptr;
+    *d_tris = nullptr;
+    info->num_nodes = 0;
+    info->num_tri_slots = 0;
+    info->depth = 0;
+    for (int k = 0; k < 3; ++k) info->bmin[k] = info->bmax[k] = 0.0f;
+    return Status();
+  }
+  TmpBufs tmp;
+  float4 *plo, *phi, *ilo, *ihi;
+  uint32_t *keys, *vals, *keys2, *vals2, *hist, *scan_tmp;
+  uint32_t *left, *right, *first, *last, *par_int, *par_leaf, *flags, *counters;
+  int* bounds;
+  uint2 *work0, *work1;
+  const uint32_t tiles = cdiv(n, RS_TILE);
+  LISA_TRY(tmp.get(&plo, n));
+  LISA_TRY(tmp.get(&phi, n));
+  LISA_TRY(tmp.get(&ilo, n));
+  LISA_TRY(tmp.get(&ihi, n));
+  LISA_TRY(tmp.get(&keys, n));
+  LISA_TRY(tmp.get(&vals, n));
+  LISA_TRY(tmp.get(&keys2, n));
+  LISA_TRY(tmp.get(&vals2, n));
+  LISA_TRY(tmp.get(&hist, 256ull * tiles));
+  LISA_TRY(tmp.get(&scan_tmp, cdiv(256ull * tiles, SCAN_CHUNK) + 16));
+  LISA_TRY(tmp.get(&left, n));
+  LISA_TRY(tmp.get(&right, n));
+  LISA_TRY(tmp.get(&first, n));
+  LISA_TRY(tmp.get(&last, n));
+  LISA_TRY(tmp.get(&par_int, n));
+  LISA_TRY(tmp.get(&par_leaf, n));
+  LISA_TRY(tmp.get(&flags, n));
+  LISA_TRY(tmp.get(&counters, 4));
+  LISA_TRY(tmp.get(&bounds, 12));
+  LISA_TRY(tmp.get(&work0, n + 1));
+  LISA_TRY(tmp.get(&work1, n + 1));
+
+  int hb[12];
+  for (int k = 0; k < 3; ++k) {
+    hb[k] = 0x7fffffff;
+    hb[3 + k] = (int)0x80000000;
+    hb[6 + k] = 0x7fffffff;
+    hb[9 + k] = (int)0x80000000;
+  }
+  LISA_CUDA(cudaMemcpyAsync(bounds, hb, sizeof(hb), cudaMemcpyHostToDevice, s));
+  const int nblk = (int)std::min<uint32_t>(cdiv(n, 256), 4096);
+  k_prim_bounds<<<nblk, 256, 0, s>>>(d_verts, n, plo, phi, bounds);
+  k_morton<<<cdiv(n, 256), 256, 0, s>>>(plo, phi, n, bounds, keys, vals);
+  LISA_CUDA(cudaGetLastError());
+  LISA_TRY(device_radix_sort(keys, vals, keys2, vals2, n, hist, scan_tmp, 32, s));
+  if (n > 1) {
+    k_karras<<<cdiv(n - 1, 256), 256, 0, s>>>(keys, n, left, right, first, last, par_int, par_leaf);
+    LISA_CUDA(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * n, s));
+    k_bottom_up<<<cdiv(n, 256), 256, 0, s>>>(n, vals, plo, phi, par_leaf, par_int, left, right, ilo, ihi, flags);
+    LISA_CUDA(cudaGetLastError());
+  }
+  // outputs
+  uint4* nodes = nullptr;
+  float4* tris = nullptr;
+  LISA_TRY(arena.alloc((void**)&nodes, sizeof(uint4) * 5ull * (n + 1), "bvh nodes"));
+  LISA_TRY(arena.alloc((void**)&tris, sizeof(float4) * 3ull * n, "bvh triangles"));
+  uint32_t hc[4] = {1u, 0u, 0u, 0u};  // node 0 is the root
+  LISA_CUDA(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
+  const uint2 root = make_uint2(0u, n > 1 ? 0u : LEAF_BIT);
+  LISA_CUDA(cudaMemcpyAsync(work0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+  CollapseArgs a{n, vals, plo, phi, ilo, ihi, left, right, first, last, d_verts, nodes, tris, counters};
+  uint32_t nwork = 1, depth = 0;
+  uint2 *wi = work0, *wo = work1;
+  while (nwork > 0) {
+    LISA_CUDA(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), s));
+    k_collapse<<<cdiv(nwork, 64), 64, 0, s>>>(a, wi, nwork, wo);
+    LISA_CUDA(cudaGetLastError());
+    LISA_CUDA(cudaMemcpyAsync(&nwork, counters + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    LISA_CUDA(cudaStreamSynchronize(s));
+    std::swap(wi, wo);
+    ++depth;
+  }
+  LISA_CUDA(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  LISA_CUDA(cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s));
+  LISA_CUDA(cudaStreamSynchronize(s));
+  if (hc[1] != n) return Status(LISA_ERR_DEVICE, "bvh build: leaf triangle count mismatch");
+  info->num_nodes = hc[0];
+  info->num_tri_slots = hc[1];
+  info->depth = depth;
+  for (int k = 0; k < 3; ++k) {
+    info->bmin[k] = ord2f(hb[k]);
+    info->bmax[k] = ord2f(hb[3 + k]);
+  }
+  *d_nodes = nodes;
+  *d_tris = tris;
+  info->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return Status();
+}
+
+}  // namespace lisa

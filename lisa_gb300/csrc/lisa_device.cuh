@@ -1,0 +1,346 @@
+// Device-side data layout and the closest-hit traversal.
+//
+// HBM layout of one scene (all arrays 16-byte aligned, read with 128-bit
+// loads):
+//   nodes  : 8-wide compressed BVH nodes, 80 B = 5 x uint4 each
+//              uint4 0: origin p.xyz (f32) | exponents ex,ey,ez (u8), imask (u8)
+//              uint4 1: child_base | tri_base | meta[0..3] | meta[4..7]
+//              uint4 2: qlo.x[8] | qlo.y[8]
+//              uint4 3: qlo.z[8] | qhi.x[8]
+//              uint4 4: qhi.y[8] | qhi.z[8]
+//            child box = p + 2^(e-127) * q (per axis); imask bit i marks an
+//            internal child at node child_base + meta[i]; a leaf child has
+//            meta[i] = count<<5 | offset (count 1..3 triangles at
+//            tri_base + offset); meta 0 and imask 0 = empty slot.
+//   tris   : 3 x float4 per leaf triangle slot, in leaf order:
+//            (v0.xyz, original triangle id as int bits), (v1, 0), (v2, 0)
+//   prims  : 5 x float4 per original triangle (shading record):
+//            (v0, n0.x) (v1, n0.y) (v2, n0.z) (n1, n2.x) (n2.y, n2.z, mat, 0)
+//   mats   : DevMaterial, 48 B each
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_math.cuh"
+
+namespace lisa {
+
+enum : int { MAT_OPAQUE = 0, MAT_DIELECTRIC = 1, MAT_EMIT = 2 };
+
+struct DevMaterial {
+  float albedo[3];
+  float roughness;
+  float emission[3];
+  float ior;
+  int cls;
+  float alpha;
+  int pad[2];
+};
+static_assert(sizeof(DevMaterial) == 48, "DevMaterial layout");
+
+constexpr float RAY_TMIN = 1e-4f;  // shader.cu:114,202
+constexpr float RAY_TMAX = 1e16f;  // shader.cu:115,202
+constexpr int NEE_TRIES = 30;      // shader.cu:199
+constexpr int TRAV_STACK = 64;
+
+enum StatusBits : uint32_t {
+  ST_STACK_OVERFLOW = 1u,
+  ST_QUEUE_OVERFLOW = 2u,
+  ST_BAD_WAVE = 4u,
+  ST_GUIDE_NONFINITE = 8u,
+};
+
+struct SceneDev {
+  const uint4* nodes;
+  const float4* tris;
+  const float4* prims;
+  const DevMaterial* mats;
+  uint32_t num_prims;
+  uint32_t num_nodes;
+  uint32_t num_mats;
+  float extent;  // bounding-box diagonal
+  uint32_t width, height;
+  uint32_t num_bounces;
+  uint32_t pad0;
+  float eye[3], U[3], V[3], W[3];
+  float lens_radius;  // 0 = pinhole
+  float focal_distance;
+  float unitU[3], unitV[3], unitW[3];
+  float bmin[3], bmax[3];  // scene bounds (guide encoding)
+  // accumulation, one entry per pixel
+  float4* acc_sum;   // Kahan sum (xyz)
+  float4* acc_comp;  // Kahan compensation (xyz)
+  double* acc_sq;    // 3 doubles: sum of squares
+  double* acc_sum64; // 3 doubles: FP64 sum (accum_fp64 only, else null)
+  uint32_t* pix_rng; // reference per-pixel stream state (LISA_RNG_PER_PIXEL)
+  int32_t guide;     // guide slot of this scene (-1 = none)
+  int32_t pad1;
+};
+
+// One group of a wave: `nplanes` consecutive sample planes of pixels
+// [pix0, pix0+npix) of one scene.  slot = slot0 + m*npix + (p - pix0).
+struct WaveGroup {
+  uint32_t scene;
+  uint32_t pix0, npix;
+  uint32_t sample0, nplanes;
+  uint32_t slot0;
+  uint32_t acc0;  // prefix of npix over the wave's groups (accumulate index)
+  uint32_t pad;
+};
+constexpr int MAX_GROUPS = 128;
+struct WaveDesc {
+  uint32_t num_groups;
+  uint32_t paths;
+  uint32_t acc_items;  // sum of npix
+  uint32_t rng_mode;
+  uint32_t seed;
+  uint32_t pad[3];
+  WaveGroup groups[MAX_GROUPS];
+};
+
+enum { HEAD_TRACE = 0, HEAD_SHADE = 1, HEAD_NEE = 2, HEAD_GUIDE = 3 };
+struct WaveCtrl {
+  uint32_t qcount[2];
+  uint32_t nee_count;
+  uint32_t train_count;
+  uint32_t head[4];
+  uint32_t status;
+  uint32_t pad[3];
+  unsigned long long rays_primary;
+  unsigned long long rays_bounce;
+  unsigned long long rays_shadow;
+  unsigned long long node_visits[2];  // [0] closest-hit stage, [1] emitter search
+  unsigned long long tri_tests[2];
+  unsigned long long nee_total;
+};
+
+// ---------------------------------------------------------------------------
+// Watertight ray/triangle test (Woop, Benthin, Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2013), evaluated with one rounding per
+// operation and no FMA so the host oracle reproduces every hit bit for bit.
+
+struct RayPre {
+  float ox, oy, oz;
+  float ix, iy, iz;  // 1/d per axis
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+  float slack;  // absolute slack on the best distance, in t units
+};
+
+__device__ __forceinline__ float sel3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
+  RayPre r;
+  r.ox = o.x;
+  r.oy = o.y;
+  r.oz = o.z;
+  r.ix = fdiv(1.0f, d.x);
+  r.iy = fdiv(1.0f, d.y);
+  r.iz = fdiv(1.0f, d.z);
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+  int kx = kz + 1;
+  if (kx == 3) kx = 0;
+  int ky = kx + 1;
+  if (ky == 3) ky = 0;
+  const float dz = sel3(d.x, d.y, d.z, kz);
+  if (dz < 0.0f) {
+    const int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  r.kx = kx;
+  r.ky = ky;
+  r.kz = kz;
+  r.Sx = fdiv(sel3(d.x, d.y, d.z, kx), dz);
+  r.Sy = fdiv(sel3(d.x, d.y, d.z, ky), dz);
+  r.Sz = fdiv(1.0f, dz);
+  const float dmax = fmaxf(ax, fmaxf(ay, az));
+  r.slack = 3.814697265625e-6f * extent / dmax;  // 2^-18 * extent / |d|max
+  return r;
+}
+
+// Returns t of the hit (or +inf).  prim_t < tbest test is the caller's.
+__device__ __forceinline__ float intersect_tri(const RayPre& r, float4 a4, float4 b4, float4 c4, float tmin) {
+  // translate to the ray origin
+  const float ax_ = fsub(a4.x, r.ox), ay_ = fsub(a4.y, r.oy), az_ = fsub(a4.z, r.oz);
+  const float bx_ = fsub(b4.x, r.ox), by_ = fsub(b4.y, r.oy), bz_ = fsub(b4.z, r.oz);
+  const float cx_ = fsub(c4.x, r.ox), cy_ = fsub(c4.y, r.oy), cz_ = fsub(c4.z, r.oz);
+  const float Akx = sel3(ax_, ay_, az_, r.kx), Aky = sel3(ax_, ay_, az_, r.ky), Akz = sel3(ax_, ay_, az_, r.kz);
+  const float Bkx = sel3(bx_, by_, bz_, r.kx), Bky = sel3(bx_, by_, bz_, r.ky), Bkz = sel3(bx_, by_, bz_, r.kz);
+  const float Ckx = sel3(cx_, cy_, cz_, r.kx), Cky = sel3(cx_, cy_, cz_, r.ky), Ckz = sel3(cx_, cy_, cz_, r.kz);
+  // shear
+  const float Axs = fsub(Akx, fmul(r.Sx, Akz)), Ays = fsub(Aky, fmul(r.Sy, Akz));
+  const float Bxs = fsub(Bkx, fmul(r.Sx, Bkz)), Bys = fsub(Bky, fmul(r.Sy, Bkz));
+  const float Cxs = fsub(Ckx, fmul(r.Sx, Ckz)), Cys = fsub(Cky, fmul(r.Sy, Ckz));
+  // scaled barycentrics (edge functions)
+  const float U = fsub(fmul(Cxs, Bys), fmul(Cys, Bxs));
+  const float V = fsub(fmul(Axs, Cys), fmul(Ays, Cxs));
+  const float W = fsub(fmul(Bxs, Ays), fmul(Bys, Axs));
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return __int_as_float(0x7f800000);
+  const float det = fadd(fadd(U, V), W);
+  if (det == 0.0f) return __int_as_float(0x7f800000);
+  const float Az = fmul(r.Sz, Akz), Bz = fmul(r.Sz, Bkz), Cz = fmul(r.Sz, Ckz);
+  const float T = fadd(fadd(fmul(U, Az), fmul(V, Bz)), fmul(W, Cz));
+  const float t = fdiv(T, det);
+  if (!(t > tmin)) return __int_as_float(0x7f800000);
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Closest-hit traversal of the 8-wide compressed BVH.  Box tests are made
+// conservative by padding each slab distance by 2^-21 (|c| + 255 |s|), which
+// bounds the rounding of q*s + c with s = 2^e/d and c = (p-o)/d, so the
+// traversal never culls a box the exact ray enters.  Candidates are culled
+// against best_t*(1+2^-16) + slack.  Together with the lowest-index tie rule
+// the result equals a brute-force scan with the same triangle test.
+
+__device__ __forceinline__ float byte_f(uint32_t w, int b) { return (float)((w >> (8 * b)) & 0xffu); }
+
+template <bool COUNT>
+__device__ __forceinline__ void closest_hit(const SceneDev& sc, V3 o, V3 d, float tmin, float tmax, int& out_prim,
+                                            float& out_t, uint32_t& visits, uint32_t& tests, uint32_t* status) {
+  out_prim = -1;
+  out_t = __int_as_float(0x7f800000);
+  if (sc.num_nodes == 0 || is_zero(d)) return;
+  const RayPre r = ray_prepare(o, d, sc.extent);
+  float best_t = tmax;
+  int best_prim = -1;  // hits need t < tmax until the first one is found
+  float cull = tmax;   // best_t * (1+2^-16) + slack (tmax itself is exact)
+  const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
+
+  uint2 stack[TRAV_STACK];
+  int sp = 0;
+  uint32_t node = 0;
+  while (true) {
+    if (COUNT) ++visits;
+    const uint4* np = sc.nodes + 5ull * node;
+    const uint4 n0 = __ldg(np + 0);
+    const uint4 n1 = __ldg(np + 1);
+    const uint4 n2 = __ldg(np + 2);
+    const uint4 n3 = __ldg(np + 3);
+    const uint4 n4 = __ldg(np + 4);
+    const float sx = __int_as_float((n0.w & 0xffu) << 23) * r.ix;
+    const float sy = __int_as_float(((n0.w >> 8) & 0xffu) << 23) * r.iy;
+    const float sz = __int_as_float(((n0.w >> 16) & 0xffu) << 23) * r.iz;
+    const float cx = (__uint_as_float(n0.x) - r.ox) * r.ix;
+    const float cy = (__uint_as_float(n0.y) - r.oy) * r.iy;
+    const float cz = (__uint_as_float(n0.z) - r.oz) * r.iz;
+    const float gx = 4.76837158203125e-7f * (fabsf(cx) + 255.0f * fabsf(sx));
+    const float gy = 4.76837158203125e-7f * (fabsf(cy) + 255.0f * fabsf(sy));
+    const float gz = 4.76837158203125e-7f * (fabsf(cz) + 255.0f * fabsf(sz));
+    const float cnx = cx - gx, cfx = cx + gx;
+    const float cny = cy - gy, cfy = cy + gy;
+    const float cnz = cz - gz, cfz = cz + gz;
+    // near/far quantised planes per axis
+    const uint32_t qlx0 = n2.x, qlx1 = n2.y, qly0 = n2.z, qly1 = n2.w;
+    const uint32_t qlz0 = n3.x, qlz1 = n3.y, qhx0 = n3.z, qhx1 = n3.w;
+    const uint32_t qhy0 = n4.x, qhy1 = n4.y, qhz0 = n4.z, qhz1 = n4.w;
+    const uint32_t nx0 = negx ? qhx0 : qlx0, nx1 = negx ? qhx1 : qlx1, fx0 = negx ? qlx0 : qhx0, fx1 = negx ? qlx1 : qhx1;
+    const uint32_t ny0 = negy ? qhy0 : qly0, ny1 = negy ? qhy1 : qly1, fy0 = negy ? qly0 : qhy0, fy1 = negy ? qly1 : qhy1;
+    const uint32_t nz0 = negz ? qhz0 : qlz0, nz1 = negz ? qhz1 : qlz1, fz0 = negz ? qlz0 : qhz0, fz1 = negz ? qlz1 : qhz1;
+    const uint32_t imask = n0.w >> 24;
+    const uint32_t child_base = n1.x, tri_base = n1.y;
+
+    uint32_t next = 0xffffffffu;
+    float next_t = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xffu;
+      const bool internal = (imask >> c) & 1u;
+      if (!internal && meta == 0) continue;
+      const int b = c & 3;
+      const float tnx = fmaf(byte_f(c < 4 ? nx0 : nx1, b), sx, cnx);
+      const float tny = fmaf(byte_f(c < 4 ? ny0 : ny1, b), sy, cny);
+      const float tnz = fmaf(byte_f(c < 4 ? nz0 : nz1, b), sz, cnz);
+      const float tfx = fmaf(byte_f(c < 4 ? fx0 : fx1, b), sx, cfx);
+      const float tfy = fmaf(byte_f(c < 4 ? fy0 : fy1, b), sy, cfy);
+      const float tfz = fmaf(byte_f(c < 4 ? fz0 : fz1, b), sz, cfz);
+      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+      const float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
+      if (!(tn <= tf)) continue;
+      if (internal) {
+        const uint32_t child = child_base + meta;
+        if (next == 0xffffffffu) {
+          next = child;
+          next_t = tn;
+        } else {
+          uint32_t push = child;
+          float push_t = tn;
+          if (tn < next_t) {
+            push = next;
+            push_t = next_t;
+            next = child;
+            next_t = tn;
+          }
+          if (sp < TRAV_STACK) {
+            stack[sp++] = make_uint2(push, __float_as_uint(push_t));
+          } else if (status) {
+            atomicOr(status, ST_STACK_OVERFLOW);
+          }
+        }
+      } else {
+        const uint32_t cnt = meta >> 5, off = meta & 31u;
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const float4* tp = sc.tris + 3ull * (tri_base + off + k);
+          const float4 a = __ldg(tp + 0), bb = __ldg(tp + 1), cc = __ldg(tp + 2);
+          if (COUNT) ++tests;
+          const float t = intersect_tri(r, a, bb, cc, tmin);
+          const int prim = __float_as_int(a.w);
+          if (t < best_t || (t == best_t && prim < best_prim)) {
+            best_t = t;
+            best_prim = prim;
+            cull = fmaf(best_t, 1.52587890625e-5f, best_t) + r.slack;
+          }
+        }
+      }
+    }
+    if (next != 0xffffffffu && next_t <= cull) {
+      node = next;
+      continue;
+    }
+    // pop
+    bool found = false;
+    while (sp > 0) {
+      const uint2 e = stack[--sp];
+      if (__uint_as_float(e.y) <= cull) {
+        node = e.x;
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+  }
+  if (best_prim >= 0) {
+    out_prim = best_prim;
+    out_t = best_t;
+  }
+}
+
+// Brute-force scan in original triangle order with the same test and tie
+// rule (lowest index wins on equal t).
+__device__ __forceinline__ void brute_hit(const SceneDev& sc, V3 o, V3 d, float tmin, float tmax, int& out_prim,
+                                          float& out_t) {
+  out_prim = -1;
+  out_t = __int_as_float(0x7f800000);
+  if (is_zero(d)) return;
+  const RayPre r = ray_prepare(o, d, sc.extent);
+  float best_t = tmax;
+  int best = -1;
+  for (uint32_t p = 0; p < sc.num_prims; ++p) {
+    const float4* pr = sc.prims + 5ull * p;
+    const float4 a = __ldg(pr + 0), b = __ldg(pr + 1), c = __ldg(pr + 2);
+    const float t = intersect_tri(r, a, b, c, tmin);
+    if (t < best_t) {
+      best_t = t;
+      best = (int)p;
+    }
+  }
+  if (best >= 0) {
+    out_prim = best;
+    out_t = best_t;
+  }
+}
+
+}  // namespace lisa

@@ -1,0 +1,168 @@
+// Host-side internals shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/lisa_gb.h"
+
+namespace lisa {
+
+// ---- status ---------------------------------------------------------------
+struct Status {
+  int code = LISA_OK;
+  std::string msg;
+  Status() = default;
+  Status(int c, std::string m) : code(c), msg(std::move(m)) {}
+  bool ok() const { return code == LISA_OK; }
+  static Status invalid(const std::string& m) { return Status(LISA_ERR_INVALID, m); }
+  static Status parse(const std::string& m) { return Status(LISA_ERR_PARSE, m); }
+  static Status io(const std::string& m) { return Status(LISA_ERR_IO, m); }
+  static Status cuda(cudaError_t e, const char* what) {
+    return Status(e == cudaErrorMemoryAllocation ? LISA_ERR_OOM : LISA_ERR_CUDA,
+                  std::string(what) + ": " + cudaGetErrorString(e));
+  }
+};
+
+#define LISA_CUDA(call)                                       \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::lisa::Status::cuda(e_, #call); \
+  } while (0)
+
+#define LISA_TRY(expr)              \
+  do {                              \
+    ::lisa::Status s_ = (expr);     \
+    if (!s_.ok()) return s_;        \
+  } while (0)
+
+// ---- parsed scene (host) ---------------------------------------------------
+struct Scene {
+  std::vector<lisa_float3> vertices;
+  std::vector<lisa_float3> normals;
+  std::vector<lisa_material> materials;
+  std::vector<int32_t> mat_indices;
+  uint32_t width = 0, height = 0, num_samples = 0, num_bounces = 0;
+  lisa_camera camera{};
+  std::string output_image;
+  std::map<std::string, int> mat_name_idx;
+};
+
+Status parse_scene_file(const std::string& path, Scene& sc);
+Status parse_scene_text(const std::string& raw, const std::string& base_dir, Scene& sc);
+Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx);
+void scene_fill_params(const Scene& sc, lisa_renderer_params* p);
+Status write_ppm_rgba8(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h);
+Status write_ppm_rgb8_flipped(const char* path, const uint8_t* rgb8, uint32_t w, uint32_t h);
+
+// ---- device allocation with an optional cap -------------------------------
+struct DeviceArena {
+  uint64_t cap = 0;
+  uint64_t used = 0;
+  std::vector<void*> blocks;
+  Status alloc(void** p, size_t bytes, const char* what);
+  void release_all();
+  ~DeviceArena() { release_all(); }
+};
+
+// ---- BVH ------------------------------------------------------------------
+struct BvhBuildResult {
+  uint32_t num_nodes = 0;
+  uint32_t num_tri_slots = 0;
+  uint32_t depth = 0;
+  double build_ms = 0.0;
+  float bmin[3], bmax[3];
+};
+
+// Builds the 8-wide compressed BVH of `num_prims` triangles whose vertices
+// are d_verts (3 float3 per triangle, device).  Outputs are allocated from
+// `arena`.
+Status build_bvh(const float* d_verts, uint32_t num_prims, cudaStream_t stream, DeviceArena& arena,
+                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info);
+
+// ---- renderer ---------------------------------------------------------------
+struct SceneDev;
+struct WaveDesc;
+struct WaveCtrl;
+struct DevMaterial;
+
+struct GuideNet;  // MLP path guide (guide.cu)
+
+struct SceneGpu {
+  lisa_renderer_params params{};  // copied (pointers not kept)
+  std::string output_image;
+  uint32_t num_prims = 0;
+  uint32_t npix = 0;
+  uint64_t samples_done = 0;  // samples per pixel accumulated
+  uint32_t subframe = 0;      // progressive launches done
+  BvhBuildResult bvh;
+  // device
+  uint4* nodes = nullptr;
+  float4* tris = nullptr;
+  float4* prims = nullptr;
+  DevMaterial* mats = nullptr;
+  float4* acc_sum = nullptr;
+  float4* acc_comp = nullptr;
+  double* acc_sq = nullptr;
+  double* acc_sum64 = nullptr;
+  uint32_t* pix_rng = nullptr;
+  float extent = 0.0f;
+  float eye[3], U[3], V[3], W[3];
+  int guide = -1;
+};
+
+struct WavePlan {
+  std::vector<std::vector<int>> dummy;
+};
+
+struct Renderer {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  lisa_options opts{};
+  DeviceArena arena;
+  std::vector<SceneGpu> scenes;
+  SceneDev* d_scenes = nullptr;
+  // wavefront buffers
+  uint32_t capacity = 0;
+  float4* ro[2] = {nullptr, nullptr};
+  float4* rd[2] = {nullptr, nullptr};
+  int2* hit = nullptr;
+  float4* ps_att = nullptr;
+  float4* ps_col = nullptr;
+  uint32_t* ps_rng = nullptr;
+  float4* nee_a = nullptr;
+  float4* nee_b = nullptr;
+  float4* nee_c = nullptr;
+  WaveCtrl* ctrl = nullptr;
+  WaveDesc* d_waves = nullptr;  // device wave table
+  uint32_t wave_capacity = 0;   // entries in d_waves
+  // launch shapes
+  int trace_blocks = 0, trace_threads = 128;
+  int nee_blocks = 0, nee_threads = 128;
+  int shade_blocks = 0, shade_threads = 256;
+  // events for stage timing
+  std::vector<cudaEvent_t> ev_pool;
+  // guided mode
+  std::vector<std::unique_ptr<GuideNet>> guides;
+  void* guide_bufs = nullptr;
+  ~Renderer();
+};
+
+Status renderer_create(const lisa_renderer_params* scenes, int n, const lisa_options* opts, Renderer** out);
+Status renderer_render(Renderer& r, uint32_t spp, bool progressive, lisa_render_stats* stats);
+Status renderer_reset(Renderer& r);
+Status renderer_get_image(Renderer& r, int scene, float* rgb32, uint8_t* rgba8, double* var, double* mean64);
+Status renderer_get_ppm(Renderer& r, int scene, uint8_t* rgb8);
+Status trace_rays(Renderer& r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t, cudaStream_t s,
+                  bool brute);
+Status trace_count(Renderer& r, const float* d_rays, uint32_t n, uint64_t* visits, uint64_t* tests);
+
+// error string per thread (api.cu)
+void set_last_error(const Status& s);
+
+}  // namespace lisa

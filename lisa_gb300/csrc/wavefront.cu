@@ -1,0 +1,888 @@
+// Wavefront path tracer: the reference estimator (src/LiSA/src/shader.cu)
+// re-organised as stages over SoA queues instead of one OptiX thread per
+// pixel.
+//
+//   raygen      one path per (scene, pixel, sample) slot          shader.cu:126-155
+//   trace       closest hit of every queued ray (persistent warps) shader.cu:77-98
+//   shade       per hit, by material class:                       shader.cu:211-255
+//                 miss / emitter -> path ends (emitter adds Le*att)
+//                 dielectric     -> Fresnel reflect / refract, next ray
+//                 opaque         -> att *= albedo, enqueue emitter search
+//   nee         up to 30 hemisphere rays per opaque vertex until one
+//               returns the (stale) emitter, then the bounce          shader.cu:196-209,248-253
+//   accumulate  per pixel, Kahan FP32 sum + FP64 sum of squares     shader.cu:156-166
+//
+// The persistent kernels take work with warp-aggregated atomics (one atomic
+// per warp per refill); queue appends are warp-aggregated the same way.
+// Counters that a stage consumes are reset by a stage that does not run
+// concurrently with it (see the comments at each reset).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "lisa_device.cuh"
+#include "lisa_internal.h"
+#include "wavefront.cuh"
+
+#ifndef LISA_BSDF_HEADER
+#define LISA_BSDF_HEADER "bsdfs/lambertian.cuh"
+#endif
+#include LISA_BSDF_HEADER
+
+namespace lisa {
+
+constexpr uint32_t FULL = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Warp-aggregated reservation of `want ? 1 : 0` entries in *counter.  All 32
+// lanes must call it.  Returns the lane's index (undefined if !want).
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, bool want) {
+  const uint32_t mask = __ballot_sync(FULL, want);
+  if (!mask) return 0;
+  const int leader = __ffs(mask) - 1;
+  const int lane = threadIdx.x & 31;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+  base = __shfl_sync(FULL, base, leader);
+  return base + __popc(mask & lanemask_lt());
+}
+
+__device__ __forceinline__ void warp_add64(unsigned long long* c, uint32_t v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(c, (unsigned long long)v);
+}
+
+__device__ __forceinline__ V3 barycentric_normal(V3 p, const float4* pr) {
+  // src/LiSA/src/maths.cu:33-56 (barycentrics re-derived from the hit point)
+  const float4 r0 = __ldg(pr + 0), r1 = __ldg(pr + 1), r2 = __ldg(pr + 2), r3 = __ldg(pr + 3), r4 = __ldg(pr + 4);
+  const V3 v1 = ld3(r0), v2 = ld3(r1), v3_ = ld3(r2);
+  const V3 n1 = v3(r0.w, r1.w, r2.w);
+  const V3 n2 = v3(r3.x, r3.y, r3.z);
+  const V3 n3 = v3(r3.w, r4.x, r4.y);
+  const V3 e1 = v2 - v1, e2 = v3_ - v1, i = p - v1;
+  const float d00 = dot(e1, e1), d01 = dot(e1, e2), d11 = dot(e2, e2);
+  const float d20 = dot(i, e1), d21 = dot(i, e2);
+  const float denom = fsub(fmul(d00, d11), fmul(d01, d01));
+  const float w = fdiv(fsub(fmul(d00, d21), fmul(d01, d20)), denom);
+  const float v = fdiv(fsub(fmul(d11, d20), fmul(d01, d21)), denom);
+  const float u = fsub(fsub(1.0f, v), w);
+  return normalize((u * n1 + v * n2) + w * n3);
+}
+
+__device__ __forceinline__ int prim_material(const SceneDev& sc, int prim) {
+  return __float_as_int(__ldg(sc.prims + 5ull * prim + 4).z);
+}
+
+__device__ __forceinline__ int find_group(const WaveDesc& w, uint32_t key, bool by_acc) {
+  int lo = 0, hi = (int)w.num_groups - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const uint32_t b = by_acc ? w.groups[mid].acc0 : w.groups[mid].slot0;
+    if (b <= key) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
+// raygen (shader.cu:126-152) -- also resets the counters of depth 0
+
+__global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
+  const WaveDesc& w = *wave;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // nothing else runs during raygen
+    b.ctrl->qcount[0] = w.paths;
+    b.ctrl->qcount[1] = 0;
+    b.ctrl->nee_count = 0;
+    b.ctrl->head[HEAD_TRACE] = 0;
+    b.ctrl->head[HEAD_SHADE] = 0;
+    b.ctrl->head[HEAD_NEE] = 0;
+    b.ctrl->rays_primary += w.paths;
+  }
+  for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < w.paths; slot += gridDim.x * blockDim.x) {
+    const WaveGroup& g = w.groups[find_group(w, slot, false)];
+    const SceneDev& sc = b.scenes[g.scene];
+    const uint32_t off = slot - g.slot0;
+    const uint32_t m = off / g.npix;
+    const uint32_t pix = g.pix0 + (off - m * g.npix);
+    const uint32_t sample = g.sample0 + m;
+    const uint32_t x = pix % sc.width, y = pix / sc.width;
+    uint32_t seed;
+    if (w.rng_mode == LISA_RNG_PER_PIXEL) {
+      seed = sc.pix_rng[pix];
+    } else {
+      seed = tea<16>(pix, tea<4>(sample, w.seed));
+    }
+    const float jx = rng11(seed);
+    const float jy = rng11(seed);
+    const float dx = fsub(fdiv(fadd(fmul(2.0f, (float)x), jx), (float)sc.width), 1.0f);
+    const float dy = fsub(fdiv(fadd(fmul(2.0f, (float)y), jy), (float)sc.height), 1.0f);
+    const V3 U = v3(sc.U[0], sc.U[1], sc.U[2]), V = v3(sc.V[0], sc.V[1], sc.V[2]), W = v3(sc.W[0], sc.W[1], sc.W[2]);
+    V3 dir = normalize((dx * U + dy * V) + W);
+    V3 org = v3(sc.eye[0], sc.eye[1], sc.eye[2]);
+    if (sc.lens_radius > 0.0f) {
+      // Thin lens (not in the reference, whose camera is a pinhole): the
+      // pinhole ray meets the focal plane at distance focal_distance along
+      // the view axis; the origin moves to a uniform point of the lens disk.
+      const V3 wu = v3(sc.unitW[0], sc.unitW[1], sc.unitW[2]);
+      const float tf = fdiv(sc.focal_distance, dot(dir, wu));
+      const V3 focus = org + tf * dir;
+      const float r = fmul(sc.lens_radius, fsqrt(rnd(seed)));
+      const float phi = fmul(6.28318530717958647692f, rnd(seed));
+      float sp, cp;
+      __sincosf(phi, &sp, &cp);
+      org = org + fmul(r, cp) * v3(sc.unitU[0], sc.unitU[1], sc.unitU[2]) +
+            fmul(r, sp) * v3(sc.unitV[0], sc.unitV[1], sc.unitV[2]);
+      dir = normalize(focus - org);
+    }
+    b.ro[0][slot] = make_float4(org.x, org.y, org.z, __uint_as_float(slot));
+    b.rd[0][slot] = make_float4(dir.x, dir.y, dir.z, RAY_TMAX);
+    b.ps_att[slot] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(-1));
+    b.ps_col[slot] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float((g.scene << 24) | pix));
+    b.ps_rng[slot] = seed;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// closest hit of the queued rays
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
+  const int q = depth & 1;
+  const uint32_t count = *(volatile uint32_t*)&b.ctrl->qcount[q];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // shade/nee of this depth have not started; the previous depth's
+    // consumers of these counters have finished
+    b.ctrl->qcount[q ^ 1] = 0;
+    b.ctrl->nee_count = 0;
+    b.ctrl->head[HEAD_SHADE] = 0;
+    b.ctrl->head[HEAD_NEE] = 0;
+    if (depth > 0) b.ctrl->rays_bounce += count;
+  }
+  const int lane = threadIdx.x & 31;
+  uint32_t visits = 0, tests = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&b.ctrl->head[HEAD_TRACE], 32u);
+    base = __shfl_sync(FULL, base, 0);
+    if (base >= count) break;
+    const uint32_t i = base + lane;
+    if (i < count) {
+      const float4 o = b.ro[q][i], d = b.rd[q][i];
+      const uint32_t slot = __float_as_uint(o.w);
+      const uint32_t scene = __float_as_uint(b.ps_col[slot].w) >> 24;
+      int prim;
+      float t;
+      closest_hit<COUNT>(b.scenes[scene], ld3(o), ld3(d), RAY_TMIN, d.w, prim, t, visits, tests, &b.ctrl->status);
+      b.hit[i] = make_int2(prim, __float_as_int(t));
+    }
+  }
+  if (COUNT) {
+    warp_add64(&b.ctrl->node_visits[0], visits);
+    warp_add64(&b.ctrl->tri_tests[0], tests);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shade: emitter / miss / dielectric / opaque (shader.cu:189-194,211-255)
+
+__global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
+  const int q = depth & 1;
+  const uint32_t count = *(volatile uint32_t*)&b.ctrl->qcount[q];
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.ctrl->head[HEAD_TRACE] = 0;  // trace of this depth is done
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t base = gw * 32; base < count; base += warps * 32) {
+    const uint32_t i = base + lane;
+    bool want_ray = false, want_nee = false;
+    V3 p = v3(0.0f), nd = v3(0.0f), N = v3(0.0f), d = v3(0.0f);
+    uint32_t slot = 0;
+    int mat_idx = 0;
+    if (i < count) {
+      const int2 h = b.hit[i];
+      const float4 o4 = b.ro[q][i];
+      slot = __float_as_uint(o4.w);
+      if (h.x >= 0) {  // a miss adds the background, 0 (optix_wrapper.cc:354-356), and ends the path
+        const float4 col = b.ps_col[slot];
+        const uint32_t scene = __float_as_uint(col.w) >> 24;
+        const SceneDev& sc = b.scenes[scene];
+        mat_idx = prim_material(sc, h.x);
+        const DevMaterial& m = sc.mats[mat_idx];
+        float4 att = b.ps_att[slot];
+        if (m.cls == MAT_EMIT) {
+          // color += Le * att; done (shader.cu:216-218)
+          const V3 c = ld3(col) + v3(m.emission[0], m.emission[1], m.emission[2]) * ld3(att);
+          b.ps_col[slot] = make_float4(c.x, c.y, c.z, col.w);
+        } else {
+          const float4 d4 = b.rd[q][i];
+          d = ld3(d4);
+          const float t = __int_as_float(h.y);
+          p = ld3(o4) + t * d;
+          N = barycentric_normal(p, sc.prims + 5ull * h.x);
+          const bool last = depth + 1 >= (int)sc.num_bounces;
+          if (m.cls == MAT_DIELECTRIC) {
+            float cosI = dot(d, N);
+            float eta;
+            V3 nrm;
+            V3 a = ld3(att);
+            if (cosI < 0.0f) {
+              cosI = -cosI;
+              eta = fdiv(1.0f, m.ior);
+              nrm = N;
+            } else {
+              a = a * v3(m.albedo[0], m.albedo[1], m.albedo[2]);
+              eta = m.ior;
+              nrm = -N;
+            }
+            uint32_t seed = b.ps_rng[slot];
+            if (eta == 1.0f) {
+              nd = d;
+            } else if (rnd(seed) <= bsdf::BTDF(cosI, eta)) {
+              nd = reflect(d, nrm);
+            } else {
+              // a zero direction (total internal reflection) is traced as a miss
+              nd = bsdf::refract(cosI, d, nrm, eta);
+            }
+            b.ps_rng[slot] = seed;
+            b.ps_att[slot] = make_float4(a.x, a.y, a.z, att.w);
+            want_ray = !last && !is_zero(nd);
+          } else {
+            const V3 a = ld3(att) * v3(m.albedo[0], m.albedo[1], m.albedo[2]);
+            b.ps_att[slot] = make_float4(a.x, a.y, a.z, att.w);
+            want_nee = true;
+          }
+        }
+      }
+    }
+    const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
+    if (want_ray) {
+      b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
+      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+    }
+    const uint32_t ni = warp_reserve(&b.ctrl->nee_count, want_nee);
+    if (want_nee) {
+      b.nee_a[ni] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
+      b.nee_b[ni] = make_float4(N.x, N.y, N.z, __int_as_float(mat_idx));
+      b.nee_c[ni] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// emitter search + bounce (shader.cu:196-209, 248-253; lambertian.cu:7-22)
+//
+// Each lane owns one opaque vertex and casts one shadow ray per loop trip;
+// a lane whose vertex finished takes the next one (warp-aggregated refill),
+// so warps stay full while vertices need between 1 and 30 rays.
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_nee(WaveBufs b, int depth) {
+  const int q = depth & 1;
+  const uint32_t count = *(volatile uint32_t*)&b.ctrl->nee_count;
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = lanemask_lt();
+  bool have = false, exhausted = false;
+  uint32_t slot = 0, tries = 0, seed = 0;
+  int stale = -1, mat_idx = 0;
+  const SceneDev* sc = nullptr;
+  V3 p = v3(0.0f), N = v3(0.0f), D = v3(0.0f), att = v3(0.0f), col = v3(0.0f);
+  float colw = 0.0f;
+  uint32_t shadow = 0, visits = 0, tests = 0;
+  while (true) {
+    const bool need = !have && !exhausted;
+    const uint32_t nmask = __ballot_sync(FULL, need);
+    if (nmask) {
+      const int leader = __ffs(nmask) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&b.ctrl->head[HEAD_NEE], (uint32_t)__popc(nmask));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        const uint32_t idx = base + __popc(nmask & lt);
+        if (idx < count) {
+          const float4 a4 = b.nee_a[idx], b4 = b.nee_b[idx], c4 = b.nee_c[idx];
+          p = ld3(a4);
+          slot = __float_as_uint(a4.w);
+          N = ld3(b4);
+          mat_idx = __float_as_int(b4.w);
+          D = ld3(c4);
+          const float4 at = b.ps_att[slot];
+          att = ld3(at);
+          stale = __float_as_int(at.w);
+          const float4 c = b.ps_col[slot];
+          col = ld3(c);
+          colw = c.w;
+          sc = b.scenes + (__float_as_uint(c.w) >> 24);
+          seed = b.ps_rng[slot];
+          tries = 0;
+          have = true;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, have)) break;
+    bool finish = false;
+    if (have) {
+      const V3 dir = bsdf::shoot_ray_hemisphere(N, seed);
+      int hp;
+      float ht;
+      closest_hit<COUNT>(*sc, p, dir, RAY_TMIN, RAY_TMAX, hp, ht, visits, tests, &b.ctrl->status);
+      ++shadow;
+      if (hp >= 0) {
+        // the occlusion hit program marks a hit only on an emitter and
+        // otherwise leaves the flag as it was (shader.cu:177-184)
+        const int hm = prim_material(*sc, hp);
+        if (sc->mats[hm].cls == MAT_EMIT) stale = hm;
+      } else {
+        stale = -1;  // miss (shader.cu:172-175)
+      }
+      if (stale >= 0) {
+        const DevMaterial& em = sc->mats[stale];
+        const DevMaterial& me = sc->mats[mat_idx];
+        const float brdf = bsdf::BRDF(N, dir, me);
+        col = col + (v3(em.emission[0], em.emission[1], em.emission[2]) * brdf) * att;
+        finish = true;
+      } else if (++tries == (uint32_t)NEE_TRIES) {
+        finish = true;
+      }
+    }
+    bool want_ray = false;
+    V3 nd = v3(0.0f);
+    if (finish) {
+      // the bounce is drawn at every vertex, the last one included, so the
+      // per-pixel stream advances exactly as in the reference
+      nd = bsdf::bounce(D, N, seed, sc->mats[mat_idx]);
+      want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
+      b.ps_rng[slot] = seed;
+      b.ps_att[slot] = make_float4(att.x, att.y, att.z, __int_as_float(stale));
+      b.ps_col[slot] = make_float4(col.x, col.y, col.z, colw);
+      have = false;
+    }
+    const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
+    if (want_ray) {
+      b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
+      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+    }
+  }
+  warp_add64(&b.ctrl->rays_shadow, shadow);
+  if (COUNT) {
+    warp_add64(&b.ctrl->node_visits[1], visits);
+    warp_add64(&b.ctrl->tri_tests[1], tests);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    b.ctrl->head[HEAD_TRACE] = 0;
+    b.ctrl->nee_total += count;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// accumulate: per pixel, the wave's samples in sample order
+
+__global__ void k_accumulate(WaveBufs b, const WaveDesc* __restrict__ wave) {
+  const WaveDesc& w = *wave;
+  for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < w.acc_items; item += gridDim.x * blockDim.x) {
+    const WaveGroup& g = w.groups[find_group(w, item, true)];
+    const SceneDev& sc = b.scenes[g.scene];
+    const uint32_t pix = g.pix0 + (item - g.acc0);
+    float4 s = sc.acc_sum[pix], c = sc.acc_comp[pix];
+    double* sq = sc.acc_sq + 3ull * pix;
+    double q0 = sq[0], q1 = sq[1], q2 = sq[2];
+    double m0 = 0, m1 = 0, m2 = 0;
+    if (sc.acc_sum64) {
+      m0 = sc.acc_sum64[3ull * pix];
+      m1 = sc.acc_sum64[3ull * pix + 1];
+      m2 = sc.acc_sum64[3ull * pix + 2];
+    }
+    uint32_t last_slot = 0;
+    for (uint32_t m = 0; m < g.nplanes; ++m) {
+      const uint32_t slot = g.slot0 + m * g.npix + (pix - g.pix0);
+      last_slot = slot;
+      const float4 v = b.ps_col[slot];
+      // Kahan: y = v - c; t = s + y; c = (t - s) - y; s = t
+      float y, t;
+      y = fsub(v.x, c.x); t = fadd(s.x, y); c.x = fsub(fsub(t, s.x), y); s.x = t;
+      y = fsub(v.y, c.y); t = fadd(s.y, y); c.y = fsub(fsub(t, s.y), y); s.y = t;
+      y = fsub(v.z, c.z); t = fadd(s.z, y); c.z = fsub(fsub(t, s.z), y); s.z = t;
+      q0 = __dadd_rn(q0, __dmul_rn((double)v.x, (double)v.x));
+      q1 = __dadd_rn(q1, __dmul_rn((double)v.y, (double)v.y));
+      q2 = __dadd_rn(q2, __dmul_rn((double)v.z, (double)v.z));
+      if (sc.acc_sum64) {
+        m0 = __dadd_rn(m0, (double)v.x);
+        m1 = __dadd_rn(m1, (double)v.y);
+        m2 = __dadd_rn(m2, (double)v.z);
+      }
+    }
+    sc.acc_sum[pix] = s;
+    sc.acc_comp[pix] = c;
+    sq[0] = q0;
+    sq[1] = q1;
+    sq[2] = q2;
+    if (sc.acc_sum64) {
+      sc.acc_sum64[3ull * pix] = m0;
+      sc.acc_sum64[3ull * pix + 1] = m1;
+      sc.acc_sum64[3ull * pix + 2] = m2;
+    }
+    if (w.rng_mode == LISA_RNG_PER_PIXEL) sc.pix_rng[pix] = b.ps_rng[last_slot];
+  }
+}
+
+__global__ void k_init_pixrng(uint32_t* rng, uint32_t npix, uint32_t subframe) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x)
+    rng[p] = tea<16>(p, subframe);  // shader.cu:141
+}
+
+// ---------------------------------------------------------------------------
+// tone map (src/cuda/helpers.h:35-62) and the PPM payload
+// (src/sutil/sutil.cpp:533-553: rows flipped, alpha dropped)
+
+__device__ __forceinline__ unsigned char quantize8(float x) {
+  x = clampf(x, 0.0f, 1.0f);
+  return (unsigned char)min((unsigned)(x * 256.0f), 255u);
+}
+__device__ __forceinline__ float to_srgb(float c) {
+  const float inv_gamma = 1.0f / 2.4f;
+  return c < 0.0031308f ? fmul(12.92f, c) : fsub(fmul(1.055f, powf(c, inv_gamma)), 0.055f);
+}
+
+__global__ void k_tonemap(const float4* __restrict__ sum, uint32_t npix, float inv_n, uint32_t width,
+                          uint32_t height, float* rgb32, uchar4* rgba8, unsigned char* ppm) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+    const float4 s = sum[p];
+    const float r = fmul(s.x, inv_n), g = fmul(s.y, inv_n), bl = fmul(s.z, inv_n);
+    if (rgb32) {
+      rgb32[3ull * p] = r;
+      rgb32[3ull * p + 1] = g;
+      rgb32[3ull * p + 2] = bl;
+    }
+    const unsigned char R = quantize8(to_srgb(clampf(r, 0.0f, 1.0f)));
+    const unsigned char G = quantize8(to_srgb(clampf(g, 0.0f, 1.0f)));
+    const unsigned char B = quantize8(to_srgb(clampf(bl, 0.0f, 1.0f)));
+    if (rgba8) rgba8[p] = make_uchar4(R, G, B, 255);
+    if (ppm) {
+      const uint32_t x = p % width, y = p / width;
+      const uint64_t o = 3ull * ((uint64_t)(height - 1 - y) * width + x);
+      ppm[o] = R;
+      ppm[o + 1] = G;
+      ppm[o + 2] = B;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// traversal hooks: closest hit / brute force / counting pass of given rays
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_rays(const SceneDev* __restrict__ scd, const float* __restrict__ rays,
+                                                   uint32_t n, int32_t* prim, float* tout, WaveCtrl* ctrl) {
+  uint32_t visits = 0, tests = 0;
+  const uint32_t total = ((n + 31) / 32) * 32;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    if (i < n) {
+      const float* r = rays + 8ull * i;
+      int hp;
+      float ht;
+      closest_hit<COUNT>(*scd, v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7], hp, ht, visits, tests,
+                         &ctrl->status);
+      if (prim) prim[i] = hp;
+      if (tout) tout[i] = ht;
+    }
+  }
+  if (COUNT) {
+    warp_add64(&ctrl->node_visits[0], visits);
+    warp_add64(&ctrl->tri_tests[0], tests);
+  }
+}
+
+__global__ void k_brute_rays(const SceneDev* __restrict__ scd, const float* __restrict__ rays, uint32_t n,
+                             int32_t* prim, float* tout) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* r = rays + 8ull * i;
+    int hp;
+    float ht;
+    brute_hit(*scd, v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7], hp, ht);
+    prim[i] = hp;
+    tout[i] = ht;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace {
+
+void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector<uint64_t>& sample_base,
+                std::vector<WaveDesc>& waves, std::vector<uint32_t>& wave_bounces) {
+  const uint32_t W = r.capacity;
+  const bool per_pixel = r.opts.rng == LISA_RNG_PER_PIXEL;
+  waves.clear();
+  wave_bounces.clear();
+  WaveDesc cur;
+  std::memset(&cur, 0, sizeof(cur));
+  uint32_t cur_b = 0;
+  auto close = [&]() {
+    if (cur.num_groups == 0) return;
+    cur.rng_mode = r.opts.rng;
+    cur.seed = r.opts.seed;
+    waves.push_back(cur);
+    wave_bounces.push_back(cur_b);
+    std::memset(&cur, 0, sizeof(cur));
+    cur_b = 0;
+  };
+  auto add = [&](uint32_t s, uint32_t pix0, uint32_t npix, uint32_t sample0, uint32_t k) {
+    WaveGroup& g = cur.groups[cur.num_groups++];
+    g.scene = s;
+    g.pix0 = pix0;
+    g.npix = npix;
+    g.sample0 = sample0;
+    g.nplanes = k;
+    g.slot0 = cur.paths;
+    g.acc0 = cur.acc_items;
+    cur.paths += k * npix;
+    cur.acc_items += npix;
+    cur_b = std::max(cur_b, r.scenes[s].params.num_bounces);
+  };
+  for (uint32_t s = 0; s < r.scenes.size(); ++s) {
+    const uint32_t npix = r.scenes[s].npix;
+    uint32_t planes = spp[s];
+    uint32_t j = (uint32_t)sample_base[s];
+    if (npix == 0 || r.scenes[s].params.num_bounces == 0) continue;
+    bool scene_in_cur = false;
+    while (planes > 0) {
+      const uint32_t room = W - cur.paths;
+      if (cur.num_groups == MAX_GROUPS || (per_pixel && scene_in_cur)) {
+        close();
+        scene_in_cur = false;
+        continue;
+      }
+      if (npix <= room) {
+        uint32_t k = std::min(planes, room / npix);
+        if (per_pixel) k = 1;
+        add(s, 0, npix, j, k);
+        scene_in_cur = true;
+        planes -= k;
+        j += k;
+      } else if (cur.paths == 0) {
+        for (uint32_t p0 = 0; p0 < npix; p0 += W) {
+          add(s, p0, std::min(W, npix - p0), j, 1);
+          close();
+        }
+        planes -= 1;
+        j += 1;
+        scene_in_cur = false;
+      } else {
+        close();
+        scene_in_cur = false;
+      }
+    }
+  }
+  close();
+}
+
+WaveBufs make_bufs(Renderer& r) {
+  WaveBufs b;
+  std::memset(&b, 0, sizeof(b));
+  b.ro[0] = r.ro[0];
+  b.ro[1] = r.ro[1];
+  b.rd[0] = r.rd[0];
+  b.rd[1] = r.rd[1];
+  b.hit = r.hit;
+  b.ps_att = r.ps_att;
+  b.ps_col = r.ps_col;
+  b.ps_rng = r.ps_rng;
+  b.nee_a = r.nee_a;
+  b.nee_b = r.nee_b;
+  b.nee_c = r.nee_c;
+  b.ctrl = r.ctrl;
+  b.scenes = r.d_scenes;
+  b.capacity = r.capacity;
+  return b;
+}
+
+struct StageTimer {
+  Renderer& r;
+  bool on;
+  size_t next = 0;
+  std::vector<std::pair<int, std::pair<size_t, size_t>>> marks;  // stage, (start ev, end ev)
+  explicit StageTimer(Renderer& rr, bool enable) : r(rr), on(enable) {}
+  Status ev(size_t* idx) {
+    if (next >= r.ev_pool.size()) {
+      cudaEvent_t e;
+      LISA_CUDA(cudaEventCreate(&e));
+      r.ev_pool.push_back(e);
+    }
+    *idx = next++;
+    LISA_CUDA(cudaEventRecord(r.ev_pool[*idx], r.stream));
+    return Status();
+  }
+};
+
+}  // namespace
+
+Status launch_wave_sequence(Renderer& r, const std::vector<uint32_t>& wave_bounces, lisa_render_stats* st,
+                            StageTimer* tm) {
+  WaveBufs b = make_bufs(r);
+  uint32_t launches[4] = {0, 0, 0, 0};  // trace, shade, nee, total
+  auto stage = [&](int which, auto&& fn) -> Status {
+    size_t e0 = 0, e1 = 0;
+    if (tm && tm->on) LISA_TRY(tm->ev(&e0));
+    fn();
+    LISA_CUDA(cudaGetLastError());
+    if (tm && tm->on) {
+      LISA_TRY(tm->ev(&e1));
+      tm->marks.push_back({which, {e0, e1}});
+    }
+    if (which < 3) launches[which]++;
+    launches[3]++;
+    return Status();
+  };
+  const int acc_blocks = r.sm_count * 8;
+  const bool counting = r.opts.count_traversal != 0;
+  for (size_t wv = 0; wv < wave_bounces.size(); ++wv) {
+    const WaveDesc* wd = r.d_waves + wv;
+    LISA_TRY(stage(3, [&] { k_raygen<<<r.sm_count * 8, 256, 0, r.stream>>>(b, wd); }));
+    for (uint32_t d = 0; d < wave_bounces[wv]; ++d) {
+      LISA_TRY(stage(0, [&] {
+        if (counting) k_trace<true><<<r.trace_blocks, r.trace_threads, 0, r.stream>>>(b, (int)d);
+        else k_trace<false><<<r.trace_blocks, r.trace_threads, 0, r.stream>>>(b, (int)d);
+      }));
+      LISA_TRY(stage(1, [&] { k_shade<<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d); }));
+      LISA_TRY(stage(2, [&] {
+        if (counting) k_nee<true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+        else k_nee<false><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+      }));
+    }
+    LISA_TRY(stage(3, [&] { k_accumulate<<<acc_blocks, 256, 0, r.stream>>>(b, wd); }));
+  }
+  if (st) {
+    st->launches_trace += launches[0];
+    st->launches_shade += launches[1];
+    st->launches_nee += launches[2];
+    st->launches_total += launches[3];
+  }
+  return Status();
+}
+
+Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_render_stats* st) {
+  lisa_render_stats local;
+  std::memset(&local, 0, sizeof(local));
+  std::vector<uint32_t> spp(r.scenes.size());
+  std::vector<uint64_t> base(r.scenes.size());
+  for (size_t s = 0; s < r.scenes.size(); ++s) {
+    spp[s] = progressive ? spp_req : r.scenes[s].params.num_samples;
+    base[s] = r.scenes[s].samples_done;
+  }
+  std::vector<WaveDesc> waves;
+  std::vector<uint32_t> wb;
+  plan_waves(r, spp, base, waves, wb);
+  if (waves.size() > r.wave_capacity) {
+    if (r.d_waves) cudaFree(r.d_waves);
+    r.d_waves = nullptr;
+    LISA_CUDA(cudaMalloc(&r.d_waves, sizeof(WaveDesc) * waves.size()));
+    r.wave_capacity = (uint32_t)waves.size();
+  }
+  if (!waves.empty())
+    LISA_CUDA(cudaMemcpyAsync(r.d_waves, waves.data(), sizeof(WaveDesc) * waves.size(), cudaMemcpyHostToDevice,
+                              r.stream));
+  // reset ray counters
+  LISA_CUDA(cudaMemsetAsync(r.ctrl, 0, sizeof(WaveCtrl), r.stream));
+  if (r.opts.rng == LISA_RNG_PER_PIXEL) {
+    for (auto& s : r.scenes) {
+      const uint32_t subframe = progressive ? s.subframe : 0u;
+      k_init_pixrng<<<r.sm_count * 4, 256, 0, r.stream>>>(s.pix_rng, s.npix, subframe);
+    }
+    LISA_CUDA(cudaGetLastError());
+  }
+  cudaEvent_t e0, e1;
+  LISA_CUDA(cudaEventCreate(&e0));
+  LISA_CUDA(cudaEventCreate(&e1));
+  LISA_CUDA(cudaEventRecord(e0, r.stream));
+  StageTimer tm(r, r.opts.stage_timing != 0);
+  Status s = launch_wave_sequence(r, wb, &local, &tm);
+  LISA_CUDA(cudaEventRecord(e1, r.stream));
+  if (!s.ok()) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return s;
+  }
+  WaveCtrl hc;
+  LISA_CUDA(cudaMemcpyAsync(&hc, r.ctrl, sizeof(hc), cudaMemcpyDeviceToHost, r.stream));
+  LISA_CUDA(cudaStreamSynchronize(r.stream));
+  float ms = 0.0f;
+  LISA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (tm.on) {
+    for (auto& m : tm.marks) {
+      float t = 0.0f;
+      LISA_CUDA(cudaEventElapsedTime(&t, r.ev_pool[m.second.first], r.ev_pool[m.second.second]));
+      if (m.first == 0) local.ms_trace += t;
+      else if (m.first == 1) local.ms_shade += t;
+      else if (m.first == 2) local.ms_nee += t;
+      else local.ms_other += t;
+    }
+  }
+  for (size_t k = 0; k < r.scenes.size(); ++k) {
+    r.scenes[k].samples_done += spp[k];
+    if (progressive) r.scenes[k].subframe++;
+  }
+  local.rays_primary = hc.rays_primary;
+  local.rays_bounce = hc.rays_bounce;
+  local.rays_shadow = hc.rays_shadow;
+  local.paths = hc.rays_primary;
+  local.samples_total = r.scenes.empty() ? 0 : r.scenes[0].samples_done;
+  local.ms_device = ms;
+  local.device_status = hc.status;
+  local.nee_vertices = hc.nee_total;
+  local.node_visits_trace = hc.node_visits[0];
+  local.tri_tests_trace = hc.tri_tests[0];
+  local.node_visits_nee = hc.node_visits[1];
+  local.tri_tests_nee = hc.tri_tests[1];
+  if (st) *st = local;
+  if (hc.status) return Status(LISA_ERR_DEVICE, "device status word " + std::to_string(hc.status));
+  return Status();
+}
+
+Status renderer_reset(Renderer& r) {
+  for (auto& s : r.scenes) {
+    LISA_CUDA(cudaMemsetAsync(s.acc_sum, 0, sizeof(float4) * s.npix, r.stream));
+    LISA_CUDA(cudaMemsetAsync(s.acc_comp, 0, sizeof(float4) * s.npix, r.stream));
+    LISA_CUDA(cudaMemsetAsync(s.acc_sq, 0, sizeof(double) * 3 * s.npix, r.stream));
+    if (s.acc_sum64) LISA_CUDA(cudaMemsetAsync(s.acc_sum64, 0, sizeof(double) * 3 * s.npix, r.stream));
+    s.samples_done = 0;
+    s.subframe = 0;
+  }
+  LISA_CUDA(cudaStreamSynchronize(r.stream));
+  return Status();
+}
+
+Status renderer_get_image(Renderer& r, int scene, float* rgb32, uint8_t* rgba8, double* var, double* mean64) {
+  if (scene < 0 || scene >= (int)r.scenes.size()) return Status::invalid("scene index out of range");
+  SceneGpu& s = r.scenes[scene];
+  const uint32_t npix = s.npix;
+  const double n = (double)s.samples_done;
+  float* d_rgb = nullptr;
+  uchar4* d_rgba = nullptr;
+  if (rgb32 || var) LISA_CUDA(cudaMalloc(&d_rgb, sizeof(float) * 3 * std::max<uint32_t>(npix, 1)));
+  if (rgba8) LISA_CUDA(cudaMalloc(&d_rgba, sizeof(uchar4) * std::max<uint32_t>(npix, 1)));
+  const float inv_n = n > 0 ? (float)(1.0 / n) : 0.0f;
+  if (npix) {
+    k_tonemap<<<r.sm_count * 4, 256, 0, r.stream>>>(s.acc_sum, npix, inv_n, s.params.width, s.params.height, d_rgb,
+                                                     d_rgba, nullptr);
+    LISA_CUDA(cudaGetLastError());
+  }
+  std::vector<float> h_rgb;
+  if (d_rgb) {
+    h_rgb.resize(3ull * npix);
+    LISA_CUDA(cudaMemcpyAsync(h_rgb.data(), d_rgb, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, r.stream));
+  }
+  if (rgba8) LISA_CUDA(cudaMemcpyAsync(rgba8, d_rgba, sizeof(uchar4) * npix, cudaMemcpyDeviceToHost, r.stream));
+  std::vector<double> sq, m64;
+  if (var) {
+    sq.resize(3ull * npix);
+    LISA_CUDA(cudaMemcpyAsync(sq.data(), s.acc_sq, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, r.stream));
+  }
+  if ((mean64 || var) && s.acc_sum64) {
+    m64.resize(3ull * npix);
+    LISA_CUDA(
+        cudaMemcpyAsync(m64.data(), s.acc_sum64, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, r.stream));
+  }
+  LISA_CUDA(cudaStreamSynchronize(r.stream));
+  if (d_rgb) cudaFree(d_rgb);
+  if (d_rgba) cudaFree(d_rgba);
+  // The mean is the float Kahan sum over n (mean of the samples); rgb32 row 0
+  // is the bottom row like the reference accum_buffer.
+  if (rgb32) std::memcpy(rgb32, h_rgb.data(), sizeof(float) * 3 * npix);
+  if (mean64) {
+    if (s.acc_sum64) {
+      for (size_t i = 0; i < 3ull * npix; ++i) mean64[i] = n > 0 ? m64[i] / n : 0.0;
+    } else {
+      for (size_t i = 0; i < 3ull * npix; ++i) mean64[i] = (double)h_rgb[i];
+    }
+  }
+  if (var) {
+    for (size_t i = 0; i < 3ull * npix; ++i) {
+      const double mu = s.acc_sum64 ? (n > 0 ? m64[i] / n : 0.0) : (double)h_rgb[i];
+      double v = n > 1 ? (sq[i] / n - mu * mu) * n / (n - 1.0) : 0.0;
+      var[i] = v > 0 ? v : 0.0;
+    }
+  }
+  return Status();
+}
+
+Status renderer_get_ppm(Renderer& r, int scene, uint8_t* rgb8) {
+  if (scene < 0 || scene >= (int)r.scenes.size()) return Status::invalid("scene index out of range");
+  SceneGpu& s = r.scenes[scene];
+  const uint32_t npix = s.npix;
+  if (npix == 0) return Status();
+  unsigned char* d = nullptr;
+  LISA_CUDA(cudaMalloc(&d, 3ull * npix));
+  const float inv_n = s.samples_done > 0 ? (float)(1.0 / (double)s.samples_done) : 0.0f;
+  k_tonemap<<<r.sm_count * 4, 256, 0, r.stream>>>(s.acc_sum, npix, inv_n, s.params.width, s.params.height, nullptr,
+                                                   nullptr, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rgb8, d, 3ull * npix, cudaMemcpyDeviceToHost, r.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return Status::cuda(e, "ppm payload");
+  return Status();
+}
+
+Status trace_rays(Renderer& r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t, cudaStream_t s,
+                  bool brute) {
+  if (r.scenes.empty()) return Status::invalid("renderer has no scene");
+  if (n == 0) return Status();
+  LISA_CUDA(cudaMemsetAsync(r.ctrl, 0, sizeof(WaveCtrl), s));
+  if (brute) {
+    k_brute_rays<<<std::min<uint32_t>((n + 127) / 128, r.sm_count * 16), 128, 0, s>>>(r.d_scenes, d_rays, n, d_prim,
+                                                                                     d_t);
+  } else {
+    k_trace_rays<false><<<std::min<uint32_t>((n + 127) / 128, r.sm_count * 16), 128, 0, s>>>(r.d_scenes, d_rays, n,
+                                                                                            d_prim, d_t, r.ctrl);
+  }
+  LISA_CUDA(cudaGetLastError());
+  uint32_t status = 0;
+  LISA_CUDA(cudaMemcpyAsync(&status, &r.ctrl->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  LISA_CUDA(cudaStreamSynchronize(s));
+  if (status) return Status(LISA_ERR_DEVICE, "device status word " + std::to_string(status));
+  return Status();
+}
+
+Status trace_count(Renderer& r, const float* d_rays, uint32_t n, uint64_t* visits, uint64_t* tests) {
+  LISA_CUDA(cudaMemsetAsync(r.ctrl, 0, sizeof(WaveCtrl), r.stream));
+  if (n)
+    k_trace_rays<true><<<std::min<uint32_t>((n + 127) / 128, r.sm_count * 16), 128, 0, r.stream>>>(
+        r.d_scenes, d_rays, n, nullptr, nullptr, r.ctrl);
+  LISA_CUDA(cudaGetLastError());
+  WaveCtrl hc;
+  LISA_CUDA(cudaMemcpyAsync(&hc, r.ctrl, sizeof(hc), cudaMemcpyDeviceToHost, r.stream));
+  LISA_CUDA(cudaStreamSynchronize(r.stream));
+  *visits = hc.node_visits[0];
+  *tests = hc.tri_tests[0];
+  return Status();
+}
+
+Status configure_launch(Renderer& r) {
+  int occ = 0;
+  const int tthreads = r.opts.threads_per_block ? (int)r.opts.threads_per_block : 128;
+  LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<false>, tthreads, 0));
+  int bps = r.opts.blocks_per_sm ? (int)r.opts.blocks_per_sm : std::max(occ, 1);
+  bps = std::min(bps, std::max(occ, 1));
+  r.trace_threads = tthreads;
+  r.trace_blocks = r.sm_count * bps;
+  LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nee<false>, tthreads, 0));
+  bps = r.opts.blocks_per_sm ? (int)r.opts.blocks_per_sm : std::max(occ, 1);
+  bps = std::min(bps, std::max(occ, 1));
+  r.nee_threads = tthreads;
+  r.nee_blocks = r.sm_count * bps;
+  LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade, 256, 0));
+  r.shade_threads = 256;
+  r.shade_blocks = r.sm_count * std::max(occ, 1);
+  return Status();
+}
+
+}  // namespace lisa

@@ -1,0 +1,34 @@
+// Kernel interfaces of the wavefront estimator (wavefront.cu) shared with
+// the guide (guide.cu) and the API layer (api.cu).
+#pragma once
+
+#include "lisa_device.cuh"
+
+namespace lisa {
+
+// Structure-of-arrays wavefront state.  A "slot" is one path in flight.
+struct WaveBufs {
+  float4* ro[2];    // ray queues (ping-pong): origin xyz, w = slot
+  float4* rd[2];    //                          direction xyz, w = tmax
+  int2* hit;        // closest hit per queued ray: (triangle, t bits)
+  float4* ps_att;   // per slot: throughput xyz, w = stale emitter material (int, -1 none)
+  float4* ps_col;   // per slot: radiance xyz,  w = scene<<24 | pixel
+  uint32_t* ps_rng; // per slot: LCG state
+  float4* nee_a;    // emitter-search queue: hit point xyz, w = slot
+  float4* nee_b;    //                       shading normal xyz, w = material
+  float4* nee_c;    //                       incoming direction xyz, w = guide flag
+  WaveCtrl* ctrl;
+  const SceneDev* scenes;
+  uint32_t capacity;
+  // guided mode (null otherwise)
+  float* guide_out;   // per NEE entry: 40 network outputs -> mixture params
+  float4* train_rec;  // per slot and depth: guide training records
+  uint32_t max_depth;
+};
+
+struct GuideSampling {
+  float bsdf_fraction;  // c in q = c p_bsdf + (1-c) p_guide
+  int enabled;
+};
+
+}  // namespace lisa

@@ -1,0 +1,71 @@
+"""The C-ABI library loads without a GPU and exports every symbol
+include/lisa_gb.h declares; reference-layout structs keep their layout."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import lisa_gb300 as L
+from lisa_gb300 import _native as N
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for hdr in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not hdr.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", hdr)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\**\s*(lisa_[a-z_0-9]+)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = N.lib()
+    names = declared_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    # and the ctypes table covers them all
+    assert set(names) <= set(N.SIGNATURES), set(names) - set(N.SIGNATURES)
+
+
+def test_reference_struct_layouts():
+    # Material: 40 bytes, offsets 0/4/8/12/24/28 (structs.hh:16-23)
+    assert C.sizeof(N.Material) == 40
+    assert [getattr(N.Material, f).offset for f in ("roughness", "alpha", "n", "diffuse_color", "emit",
+                                                     "emission_color")] == [0, 4, 8, 12, 24, 28]
+    assert C.sizeof(N.Camera) == 28
+    assert C.sizeof(N.Options) == N.default_options().struct_size
+
+
+def test_errors_without_gpu_are_reported_not_raised():
+    lib = N.lib()
+    assert lib.lisa_version().startswith(b"lisa_gb300")
+    # bad arguments come back as status codes with a message
+    assert lib.lisa_scene_parse(None, None) == N.LISA_ERR_INVALID
+    assert b"null" in lib.lisa_last_error()
+    assert lib.lisa_render(None, None) == N.LISA_ERR_INVALID
+
+
+def test_ppm_writer_matches_save_image_layout(tmp_path):
+    import numpy as np
+
+    rgba = np.zeros((3, 4, 4), np.uint8)
+    rgba[..., 0] = np.arange(3)[:, None] * 10  # row index in red
+    rgba[..., 1] = np.arange(4)[None, :]
+    rgba[..., 3] = 255
+    p = tmp_path / "a.ppm"
+    L.write_ppm(str(p), rgba)
+    data = p.read_bytes()
+    assert data.startswith(b"P6\n4 3\n255\n")
+    pix = np.frombuffer(data[len(b"P6\n4 3\n255\n"):], np.uint8).reshape(3, 4, 3)
+    # rows flipped (sutil.cpp:543-553), alpha dropped
+    assert pix[0, 0, 0] == 20 and pix[2, 0, 0] == 0
+    assert pix[1, 3, 1] == 3
+    with pytest.raises(L.LisaError):
+        L.write_ppm(str(tmp_path / "a.png"), rgba)

@@ -1,0 +1,139 @@
+"""The wavefront estimator on the GPU against the CPU oracle.
+
+Both restate the reference estimator (src/LiSA/src/shader.cu) with the same
+RNG streams and the same IEEE operation order, so at small sizes every path
+agrees: per-pixel means equal up to the float accumulation (tolerance
+1e-5 relative) and the ray counts are identical.  With different streams
+the two are independent estimates of the same image: per-pixel means agree
+within 3 sigma (sigma from the per-pixel FP64 variances).
+"""
+import numpy as np
+import pytest
+
+import lisa_gb300 as L
+from lisa_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_mean(oracle, sc, **kw):
+    s, q, rays = oracle.Scene.from_scene(sc, **kw).render(use_bvh=True)
+    spp = kw.get("spp", sc.num_samples)
+    mean = s / spp
+    var = np.maximum(q / spp - mean * mean, 0.0) * spp / max(spp - 1, 1)
+    return mean.reshape(sc.height, sc.width, 3), var.reshape(sc.height, sc.width, 3), rays
+
+
+def mismatch_fraction(a, b, rtol=1e-5):
+    bad = np.abs(a - b) > rtol * np.maximum(1.0, np.abs(b))
+    return bad.any(axis=2).mean()
+
+
+def test_path_by_path_cornell_box(gpu, oracle):
+    sc = scenes.cornell_box(width=48, height=32, num_samples=4, num_bounces=7)
+    r = L.Renderer(L.params_from_scene(sc))
+    st = r.render()
+    img = r.image()
+    ref, _, rays = oracle_mean(oracle, sc)
+    assert mismatch_fraction(img, ref) <= 0.002
+    assert st.rays_primary == rays[0]
+    assert abs(int(st.rays_bounce) - int(rays[1])) <= 0.002 * rays[1]
+    assert abs(int(st.rays_shadow) - int(rays[2])) <= 0.002 * rays[2]
+    assert st.device_status == 0
+
+
+def test_path_by_path_reference_stream(gpu, oracle):
+    """LISA_RNG_PER_PIXEL: one tea<16>(pixel, subframe) stream per pixel
+    shared by its samples, exactly the reference raygen (shader.cu:141-155)."""
+    sc = scenes.cornell_box(width=32, height=24, num_samples=3, num_bounces=5)
+    r = L.Renderer(L.params_from_scene(sc), rng=L._native.LISA_RNG_PER_PIXEL)
+    r.render()
+    img = r.image()
+    ref, _, _ = oracle_mean(oracle, sc, rng_mode=1)
+    assert mismatch_fraction(img, ref) <= 0.002
+
+
+def test_statistical_agreement_independent_streams(gpu, oracle):
+    sc = scenes.cornell_box(width=40, height=40, num_samples=256, num_bounces=7)
+    r = L.Renderer(L.params_from_scene(sc), seed=7)
+    r.render()
+    img, var = r.image(variance=True)
+    ref, rvar, _ = oracle_mean(oracle, sc, seed=99)
+    n = sc.num_samples
+    sigma = np.sqrt(var / n + rvar / n)
+    z = np.abs(img - ref) / np.maximum(sigma, 1e-12)
+    z[(sigma == 0) & (np.abs(img - ref) == 0)] = 0
+    frac = (z > 3).mean()
+    assert frac < 0.02, frac
+    # the two images are not the same draw
+    assert mismatch_fraction(img, ref) > 0.5
+
+
+def test_progressive_equals_batch(gpu):
+    """Two progressive launches of 2 spp equal one batch of 4 spp (same
+    sample indices, same Kahan order) -- the reference's subframe lerp
+    (shader.cu:160-164) is the running mean."""
+    sc = scenes.cornell_box(width=32, height=32, num_samples=4, num_bounces=4)
+    a = L.Renderer(L.params_from_scene(sc))
+    a.render()
+    b = L.Renderer(L.params_from_scene(sc))
+    b.render_progressive(2)
+    st = b.render_progressive(2)
+    assert st.samples_total == 4
+    assert np.array_equal(a.image(), b.image())
+    b.reset()
+    b.render_progressive(4)
+    assert np.array_equal(a.image(), b.image())
+
+
+def test_ppm_payload_and_file(gpu, oracle, tmp_path):
+    sc = scenes.cornell_box(width=40, height=30, num_samples=8, num_bounces=5)
+    r = L.Renderer(L.params_from_scene(sc, output_image=str(tmp_path / "img.ppm")))
+    L.render(r)
+    img = r.image()
+    rgba = r.rgba8()
+    ref = oracle.make_color(img.reshape(-1, 3)).reshape(sc.height, sc.width, 4)
+    diff = np.abs(rgba.astype(int) - ref.astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() < 0.01  # device powf vs host powf
+    payload = r.ppm_rgb8()
+    assert np.array_equal(payload, rgba[::-1, :, :3])
+    data = (tmp_path / "img.ppm").read_bytes()
+    hdr = f"P6\n{sc.width} {sc.height}\n255\n".encode()
+    assert data.startswith(hdr) and data[len(hdr):] == payload.tobytes()
+
+
+def test_batch_of_uneven_scenes_matches_single_renders(gpu):
+    a = scenes.cornell_box(width=24, height=16, num_samples=2, num_bounces=3)
+    b = scenes.icosphere_box(level=3, width=20, height=20, num_samples=3, num_bounces=5)
+    batch = L.Renderer([L.params_from_scene(a), L.params_from_scene(b)], paths_in_flight=700)
+    batch.render()
+    for k, sc in enumerate((a, b)):
+        single = L.Renderer(L.params_from_scene(sc))
+        single.render()
+        assert np.array_equal(batch.image(k), single.image()), k
+
+
+def test_wave_splitting_small_capacity(gpu):
+    """A capacity smaller than one image plane splits planes into pixel
+    ranges; the result is unchanged."""
+    sc = scenes.cornell_box(width=37, height=23, num_samples=3, num_bounces=4)
+    a = L.Renderer(L.params_from_scene(sc))
+    a.render()
+    b = L.Renderer(L.params_from_scene(sc), paths_in_flight=100)
+    b.render()
+    assert np.array_equal(a.image(), b.image())
+
+
+def test_errors_are_status_codes(gpu):
+    sc = scenes.cornell_box(width=8, height=8, num_samples=1)
+    v, n, mi = sc.soup()
+    mi = mi.copy()
+    mi[3] = 99  # material index out of range
+    p = L.params_from_arrays(v, n, mi, sc.material_table(), 8, 8, sc.eye, sc.look_at, sc.fov, 1, 2)
+    with pytest.raises(L.LisaError) as e:
+        L.Renderer(p)
+    assert e.value.code == L._native.LISA_ERR_INVALID
+    # an allocation cap turns into LISA_ERR_OOM, not a crash
+    with pytest.raises(L.LisaError) as e:
+        L.Renderer(L.params_from_scene(sc), alloc_cap_bytes=1024)
+    assert e.value.code == L._native.LISA_ERR_OOM

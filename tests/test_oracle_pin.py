@@ -1,0 +1,156 @@
+"""Pins the CPU oracle against golden vectors of the reference's own code.
+
+tests/golden/ref_math.txt holds outputs of the reference's device helpers
+compiled on the host from its sources (oracle/ref_kernels_dump.cc:
+random.h, vec_math.h, maths.cu, bsdfs/lambertian.cu, helpers.h,
+Camera.cpp).  The oracle restates those functions; this test shows the
+restatement computes the same values: bit for bit where the arithmetic is
+the same, within a stated tolerance where the oracle deliberately differs
+(pow(x,2)/pow(x,5) as products and pi as a float constant, where the
+host-compiled reference rounds through double).
+"""
+import ctypes as C
+import os
+import struct
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden", "ref_math.txt")
+
+
+def f(h: str) -> float:
+    return struct.unpack("<f", struct.pack("<I", int(h, 16)))[0]
+
+
+def fa(hs):
+    return np.array([f(h) for h in hs], np.float32)
+
+
+def records(name):
+    with open(GOLD) as fh:
+        for line in fh:
+            parts = line.split()
+            if parts and parts[0] == name:
+                yield parts[1:]
+
+
+def ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+def test_golden_file_complete():
+    names = {}
+    with open(GOLD) as fh:
+        for line in fh:
+            names[line.split()[0]] = names.get(line.split()[0], 0) + 1
+    for k in ("tea16", "rnd", "normalize", "reflect", "faceforward", "lerp", "fresnel", "refract", "brdf",
+              "bounce0", "barynormal", "make_color", "uvw"):
+        assert names.get(k, 0) > 0, k
+
+
+def test_tea16(oracle):
+    L = oracle.lib()
+    n = 0
+    for a, b, v in records("tea16"):
+        assert L.oracle_tea16(int(a, 16), int(b, 16)) == int(v, 16)
+        n += 1
+    assert n >= 40
+
+
+def test_rnd_stream(oracle):
+    L = oracle.lib()
+    for rec in records("rnd"):
+        s = C.c_uint32(int(rec[0], 16))
+        got = [L.oracle_rnd(C.byref(s)) for _ in range(8)]
+        assert np.array_equal(np.array(got, np.float32), fa(rec[1:9]))
+        assert s.value == int(rec[9], 16)
+
+
+def test_vector_helpers_bit_exact(oracle):
+    L = oracle.lib()
+    out = np.empty(3, np.float32)
+    for rec in records("normalize"):
+        a = fa(rec[0:3])
+        L.oracle_normalize(ptr(a), ptr(out))
+        assert np.array_equal(out, fa(rec[3:6]))
+    for rec in records("reflect"):
+        a, b = fa(rec[0:3]), fa(rec[3:6])
+        L.oracle_reflect(ptr(a), ptr(b), ptr(out))
+        assert np.array_equal(out, fa(rec[6:9]))
+    for rec in records("faceforward"):
+        a, b = fa(rec[0:3]), fa(rec[3:6])
+        L.oracle_faceforward(ptr(a), ptr(b), ptr(a), ptr(out))
+        assert np.array_equal(out, fa(rec[6:9]))
+    for rec in records("lerp"):
+        a, b, t = fa(rec[0:3]), fa(rec[3:6]), f(rec[6])
+        L.oracle_lerp(ptr(a), ptr(b), C.c_float(t), ptr(out))
+        assert np.array_equal(out, fa(rec[7:10]))
+
+
+def test_fresnel_within_tolerance(oracle):
+    # reference: pow() in double on the host (fast-math __powf on the GPU);
+    # oracle: products in float.  Tolerance 4e-7 absolute on values in [0,1].
+    L = oracle.lib()
+    for rec in records("fresnel"):
+        c, eta, ref = f(rec[0]), f(rec[1]), f(rec[2])
+        assert abs(L.oracle_fresnel(C.c_float(c), C.c_float(eta)) - ref) <= 4e-7
+
+
+def test_refract_bit_exact(oracle):
+    L = oracle.lib()
+    out = np.empty(3, np.float32)
+    for rec in records("refract"):
+        cosI, d, n, eta = f(rec[0]), fa(rec[1:4]), fa(rec[4:7]), f(rec[7])
+        L.oracle_refract(C.c_float(cosI), ptr(d), ptr(n), C.c_float(eta), ptr(out))
+        assert np.array_equal(out, fa(rec[8:11]))
+
+
+def test_brdf_within_tolerance(oracle):
+    # reference divides by M_PI in double; oracle by pi rounded to float.
+    L = oracle.lib()
+    for rec in records("brdf"):
+        n, l_, ref = fa(rec[0:3]), fa(rec[3:6]), f(rec[6])
+        got = L.oracle_brdf(ptr(n), ptr(l_))
+        assert abs(got - ref) <= 2.0 * np.spacing(np.float32(max(abs(ref), 1e-30)))
+
+
+def test_bounce_roughness0_and_stream(oracle):
+    """bounce() with roughness 0 is the mirror direction and still consumes
+    the three hemisphere draws (lambertian.cu:7-13)."""
+    L = oracle.lib()
+    out = np.empty(3, np.float32)
+    for i, rec in enumerate(records("bounce0")):
+        d, n = fa(rec[0:3]), fa(rec[3:6])
+        L.oracle_reflect(ptr(d), ptr(n), ptr(out))
+        assert np.array_equal(out, fa(rec[6:9]))
+        s = C.c_uint32(1000 + i)
+        hemi = np.empty(3, np.float32)
+        L.oracle_hemi(ptr(n), C.byref(s), ptr(hemi))
+        assert s.value == int(rec[9], 16)
+
+
+def test_barycentric_normal_bit_exact(oracle):
+    L = oracle.lib()
+    out = np.empty(3, np.float32)
+    for rec in records("barynormal"):
+        p, n9, v9 = fa(rec[0:3]), fa(rec[3:12]), fa(rec[12:21])
+        L.oracle_barycentric_normal(ptr(p), ptr(n9), ptr(v9), ptr(out))
+        assert np.array_equal(out, fa(rec[21:24]))
+
+
+def test_make_color_bit_exact(oracle):
+    rgb = np.stack([fa(rec[0:3]) for rec in records("make_color")])
+    ref = np.array([[int(x, 16) for x in rec[3:7]] for rec in records("make_color")], np.uint8)
+    assert np.array_equal(oracle.make_color(rgb), ref)
+
+
+def test_camera_frame_bit_exact(oracle):
+    L = oracle.lib()
+    out = np.empty(9, np.float32)
+    for rec in records("uvw"):
+        eye, look, fov = fa(rec[0:3]), fa(rec[3:6]), f(rec[6])
+        w, h = int(rec[7]), int(rec[8])
+        L.oracle_uvw(ptr(eye), ptr(look), C.c_float(fov), w, h, ptr(out))
+        assert np.array_equal(out, fa(rec[9:18]))
