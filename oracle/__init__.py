@@ -50,6 +50,10 @@ def lib():
         P = C.c_void_p
         L.oracle_closest.argtypes = [P, C.c_uint32, P, C.c_uint32, C.c_int, C.c_int, P, P]
         L.oracle_render.argtypes = [C.POINTER(OracleScene), C.c_int, C.c_int, C.c_uint32, C.c_uint32, P, P, P]
+        L.oracle_ctx_create.restype = C.c_void_p
+        L.oracle_ctx_create.argtypes = [C.POINTER(OracleScene), C.c_int]
+        L.oracle_ctx_destroy.argtypes = [P]
+        L.oracle_ctx_render.argtypes = [P, C.POINTER(OracleScene), C.c_int, C.c_uint32, C.c_uint32, P, P, P]
         L.oracle_make_color.argtypes = [P, C.c_uint64, P]
         L.oracle_tea16.restype = C.c_uint32
         L.oracle_tea16.argtypes = [C.c_uint32, C.c_uint32]
@@ -117,15 +121,28 @@ class Scene:
         return cls(v, n, mi, scene.material_table(), **args)
 
     def render(self, px0=0, px1=None, use_bvh=True, threads=0):
-        """FP64 per-pixel sums over spp samples: (sum, sumsq, rays[3])."""
+        """FP64 per-pixel sums over spp samples: (sum, sumsq, rays[3]).  The
+        scene context (CPU BVH) is built on the first call and reused."""
         npix = self.s.width * self.s.height
         px1 = npix if px1 is None else px1
         k = px1 - px0
-        s = np.zeros((k, 3), np.float64)
-        q = np.zeros((k, 3), np.float64)
+        s = np.zeros((max(k, 0), 3), np.float64)
+        q = np.zeros((max(k, 0), 3), np.float64)
         rays = np.zeros(3, np.uint64)
-        lib().oracle_render(C.byref(self.s), int(use_bvh), int(threads), px0, px1, _p(s), _p(q), _p(rays))
+        ctx = self._ctx(bool(use_bvh))
+        lib().oracle_ctx_render(ctx, C.byref(self.s), int(threads), px0, px1, _p(s), _p(q), _p(rays))
         return s, q, rays
+
+    def _ctx(self, use_bvh: bool):
+        cache = self.__dict__.setdefault("_ctxs", {})
+        if use_bvh not in cache:
+            cache[use_bvh] = lib().oracle_ctx_create(C.byref(self.s), int(use_bvh))
+        return cache[use_bvh]
+
+    def __del__(self):
+        for c in self.__dict__.get("_ctxs", {}).values():
+            if c:
+                lib().oracle_ctx_destroy(c)
 
 
 def closest(vertices, rays, use_bvh=False, threads=0):

@@ -502,6 +502,17 @@ int oracle_closest(const float* verts, uint32_t T, const float* rays, uint32_t n
   return 0;
 }
 
+// A scene context (material table, CPU BVH) reusable across render calls.
+void* oracle_ctx_create(const oracle_scene* s, int use_bvh) {
+  Ctx* c = new Ctx();
+  make_ctx(s, use_bvh, *c);
+  return c;
+}
+void oracle_ctx_destroy(void* c) { delete (Ctx*)c; }
+
+int oracle_ctx_render(void* ctx, const oracle_scene* s, int threads, uint32_t px0, uint32_t px1, double* sum,
+                      double* sumsq, uint64_t* rays);
+
 // Render pixels [px0, px1) of the scene: per pixel the FP64 sum and sum of
 // squares of the spp sample radiances (3 doubles each).  rays[3] receives
 // primary, bounce and shadow ray counts.
@@ -509,6 +520,12 @@ int oracle_render(const oracle_scene* s, int use_bvh, int threads, uint32_t px0,
                   double* sumsq, uint64_t* rays) {
   Ctx c;
   make_ctx(s, use_bvh, c);
+  return oracle_ctx_render(&c, s, threads, px0, px1, sum, sumsq, rays);
+}
+
+int oracle_ctx_render(void* ctx, const oracle_scene* s, int threads, uint32_t px0, uint32_t px1, double* sum,
+                      double* sumsq, uint64_t* rays) {
+  const Ctx& c = *(const Ctx*)ctx;
   V3 U, V, W;
   uvw(s->eye, s->look_at, s->fov, s->width, s->height, U, V, W);
   const V3 eye = v3(s->eye[0], s->eye[1], s->eye[2]);
