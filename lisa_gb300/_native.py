@@ -115,6 +115,7 @@ SIGNATURES = {
     "lisa_trace_closest_device": (C.c_int, [_P, _P, C.c_uint32, _P, _P, _P]),
     "lisa_trace_brute_device": (C.c_int, [_P, _P, C.c_uint32, _P, _P, _P]),
     "lisa_trace_count": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "lisa_trace_soup_noalloc": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, _P, _P]),
     "lisa_bvh_info": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
     "lisa_guide_create": (C.c_int, [C.c_uint32, C.POINTER(_P)]),

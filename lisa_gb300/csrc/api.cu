@@ -65,6 +65,30 @@ void DeviceArena::release_all() {
   used = 0;
 }
 
+Status TempDeviceBufs::get(void** p, size_t bytes, const char* what) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(bytes, 16));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return Status(LISA_ERR_OOM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+  }
+  ptrs.push_back(q);
+  *p = q;
+  return Status();
+}
+
+TempDeviceBufs::~TempDeviceBufs() {
+  for (void* p : ptrs) cudaFree(p);
+}
+
+Status BumpScratch::get(void** p, size_t bytes, const char* what) {
+  const size_t need = (std::max<size_t>(bytes, 16) + 255) & ~(size_t)255;
+  if (used + need > size) return Status(LISA_ERR_OOM, std::string("scratch region too small for ") + what);
+  *p = base + used;
+  used += need;
+  return Status();
+}
+
 Renderer::~Renderer() {
   if (stream) cudaStreamSynchronize(stream);
   for (auto e : ev_pool) cudaEventDestroy(e);
@@ -181,8 +205,12 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
       return Status::cuda(e, "pack triangles");
     }
   }
-  Status st = build_bvh(d_v, T, r.stream, r.arena, &s.nodes, &s.tris, &s.bvh);
-  cudaStreamSynchronize(r.stream);
+  Status st;
+  {
+    TempDeviceBufs tmp;
+    st = build_bvh(d_v, T, r.stream, tmp, r.arena, &s.nodes, &s.tris, &s.bvh);
+    cudaStreamSynchronize(r.stream);
+  }
   if (d_v) cudaFree(d_v);
   if (d_n) cudaFree(d_n);
   if (d_m) cudaFree(d_m);

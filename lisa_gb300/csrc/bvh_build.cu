@@ -517,24 +517,32 @@ Status device_radix_sort(uint32_t* keys, uint32_t* vals, uint32_t* keys2, uint32
 }
 
 namespace {
-struct TmpBufs {
-  std::vector<void*> ptrs;
-  ~TmpBufs() {
-    for (void* p : ptrs) cudaFree(p);
-  }
-  template <class T>
-  Status get(T** p, size_t count) {
-    void* q = nullptr;
-    LISA_CUDA(cudaMalloc(&q, std::max<size_t>(count * sizeof(T), 16)));
-    ptrs.push_back(q);
-    *p = (T*)q;
-    return Status();
-  }
-};
+template <class T>
+Status take(ScratchSource& src, T** p, uint64_t count, const char* what) {
+  void* q = nullptr;
+  LISA_TRY(src.get(&q, std::max<uint64_t>(count * sizeof(T), 16), what));
+  *p = (T*)q;
+  return Status();
+}
+inline uint64_t al256(uint64_t b) { return (std::max<uint64_t>(b, 16) + 255) & ~255ull; }
 }  // namespace
 
-Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, DeviceArena& arena, uint4** d_nodes,
-                 float4** d_tris, BvhBuildResult* info) {
+size_t bvh_temp_bytes(uint32_t n) {
+  const uint64_t tiles = cdiv(n, RS_TILE);
+  uint64_t b = 0;
+  b += 4 * al256(16ull * n);                                   // plo phi ilo ihi
+  b += 4 * al256(4ull * n);                                    // keys vals keys2 vals2
+  b += al256(4ull * 256 * tiles) + al256(4ull * (cdiv(256ull * tiles, SCAN_CHUNK) + 16));
+  b += 7 * al256(4ull * n);                                    // tree links and flags
+  b += al256(16) + al256(48);                                  // counters, bounds
+  b += 2 * al256(8ull * (n + 1));                              // collapse work lists
+  return (size_t)b;
+}
+
+size_t bvh_output_bytes(uint32_t n) { return (size_t)(al256(80ull * (n + 1)) + al256(48ull * n)); }
+
+Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource& tmp, ScratchSource& out,
+                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info) {
   auto t0 = std::chrono::steady_clock::now();
   if (n == 0) {
     *d_nodes = nullptr;
@@ -545,34 +553,34 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, DeviceArena& 
     for (int k = 0; k < 3; ++k) info->bmin[k] = info->bmax[k] = 0.0f;
     return Status();
   }
-  TmpBufs tmp;
   float4 *plo, *phi, *ilo, *ihi;
   uint32_t *keys, *vals, *keys2, *vals2, *hist, *scan_tmp;
   uint32_t *left, *right, *first, *last, *par_int, *par_leaf, *flags, *counters;
   int* bounds;
   uint2 *work0, *work1;
   const uint32_t tiles = cdiv(n, RS_TILE);
-  LISA_TRY(tmp.get(&plo, n));
-  LISA_TRY(tmp.get(&phi, n));
-  LISA_TRY(tmp.get(&ilo, n));
-  LISA_TRY(tmp.get(&ihi, n));
-  LISA_TRY(tmp.get(&keys, n));
-  LISA_TRY(tmp.get(&vals, n));
-  LISA_TRY(tmp.get(&keys2, n));
-  LISA_TRY(tmp.get(&vals2, n));
-  LISA_TRY(tmp.get(&hist, 256ull * tiles));
-  LISA_TRY(tmp.get(&scan_tmp, cdiv(256ull * tiles, SCAN_CHUNK) + 16));
-  LISA_TRY(tmp.get(&left, n));
-  LISA_TRY(tmp.get(&right, n));
-  LISA_TRY(tmp.get(&first, n));
-  LISA_TRY(tmp.get(&last, n));
-  LISA_TRY(tmp.get(&par_int, n));
-  LISA_TRY(tmp.get(&par_leaf, n));
-  LISA_TRY(tmp.get(&flags, n));
-  LISA_TRY(tmp.get(&counters, 4));
-  LISA_TRY(tmp.get(&bounds, 12));
-  LISA_TRY(tmp.get(&work0, n + 1));
-  LISA_TRY(tmp.get(&work1, n + 1));
+  const char* w = "bvh build scratch";
+  LISA_TRY(take(tmp, &plo, n, w));
+  LISA_TRY(take(tmp, &phi, n, w));
+  LISA_TRY(take(tmp, &ilo, n, w));
+  LISA_TRY(take(tmp, &ihi, n, w));
+  LISA_TRY(take(tmp, &keys, n, w));
+  LISA_TRY(take(tmp, &vals, n, w));
+  LISA_TRY(take(tmp, &keys2, n, w));
+  LISA_TRY(take(tmp, &vals2, n, w));
+  LISA_TRY(take(tmp, &hist, 256ull * tiles, w));
+  LISA_TRY(take(tmp, &scan_tmp, cdiv(256ull * tiles, SCAN_CHUNK) + 16, w));
+  LISA_TRY(take(tmp, &left, n, w));
+  LISA_TRY(take(tmp, &right, n, w));
+  LISA_TRY(take(tmp, &first, n, w));
+  LISA_TRY(take(tmp, &last, n, w));
+  LISA_TRY(take(tmp, &par_int, n, w));
+  LISA_TRY(take(tmp, &par_leaf, n, w));
+  LISA_TRY(take(tmp, &flags, n, w));
+  LISA_TRY(take(tmp, &counters, 4, w));
+  LISA_TRY(take(tmp, &bounds, 12, w));
+  LISA_TRY(take(tmp, &work0, n + 1, w));
+  LISA_TRY(take(tmp, &work1, n + 1, w));
 
   int hb[12];
   for (int k = 0; k < 3; ++k) {
@@ -596,8 +604,8 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, DeviceArena& 
   // outputs
   uint4* nodes = nullptr;
   float4* tris = nullptr;
-  LISA_TRY(arena.alloc((void**)&nodes, sizeof(uint4) * 5ull * (n + 1), "bvh nodes"));
-  LISA_TRY(arena.alloc((void**)&tris, sizeof(float4) * 3ull * n, "bvh triangles"));
+  LISA_TRY(take(out, &nodes, 5ull * (n + 1), "bvh nodes"));
+  LISA_TRY(take(out, &tris, 3ull * n, "bvh triangles"));
   uint32_t hc[4] = {1u, 0u, 0u, 0u};  // node 0 is the root
   LISA_CUDA(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
   const uint2 root = make_uint2(0u, n > 1 ? 0u : LEAF_BIT);

@@ -59,14 +59,38 @@ void scene_fill_params(const Scene& sc, lisa_renderer_params* p);
 Status write_ppm_rgba8(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h);
 Status write_ppm_rgb8_flipped(const char* path, const uint8_t* rgb8, uint32_t w, uint32_t h);
 
-// ---- device allocation with an optional cap -------------------------------
-struct DeviceArena {
+// ---- device memory sources ---------------------------------------------------
+// Where a builder takes its device buffers from: cudaMalloc (DeviceArena,
+// TempDeviceBufs) or a caller-provided region (BumpScratch).
+struct ScratchSource {
+  virtual Status get(void** p, size_t bytes, const char* what) = 0;
+  virtual ~ScratchSource() = default;
+};
+
+// cudaMalloc with an optional cap; blocks live until release_all().
+struct DeviceArena : ScratchSource {
   uint64_t cap = 0;
   uint64_t used = 0;
   std::vector<void*> blocks;
   Status alloc(void** p, size_t bytes, const char* what);
+  Status get(void** p, size_t bytes, const char* what) override { return alloc(p, bytes, what); }
   void release_all();
-  ~DeviceArena() { release_all(); }
+  ~DeviceArena() override { release_all(); }
+};
+
+// cudaMalloc'd temporaries freed when the object goes out of scope.
+struct TempDeviceBufs : ScratchSource {
+  std::vector<void*> ptrs;
+  Status get(void** p, size_t bytes, const char* what) override;
+  ~TempDeviceBufs() override;
+};
+
+// Carves 256-byte aligned pieces out of one existing device region.
+struct BumpScratch : ScratchSource {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  BumpScratch(void* b, size_t s) : base((char*)b), size(s) {}
+  Status get(void** p, size_t bytes, const char* what) override;
 };
 
 // ---- BVH ------------------------------------------------------------------
@@ -79,10 +103,13 @@ struct BvhBuildResult {
 };
 
 // Builds the 8-wide compressed BVH of `num_prims` triangles whose vertices
-// are d_verts (3 float3 per triangle, device).  Outputs are allocated from
-// `arena`.
-Status build_bvh(const float* d_verts, uint32_t num_prims, cudaStream_t stream, DeviceArena& arena,
-                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info);
+// are d_verts (3 float3 per triangle, device).  Temporaries come from `tmp`,
+// the node and leaf-triangle arrays from `out`.
+Status build_bvh(const float* d_verts, uint32_t num_prims, cudaStream_t stream, ScratchSource& tmp,
+                 ScratchSource& out, uint4** d_nodes, float4** d_tris, BvhBuildResult* info);
+// Device bytes build_bvh takes from `tmp` and from `out` for n triangles.
+size_t bvh_temp_bytes(uint32_t n);
+size_t bvh_output_bytes(uint32_t n);
 
 // ---- renderer ---------------------------------------------------------------
 struct SceneDev;
@@ -161,6 +188,10 @@ Status renderer_get_ppm(Renderer& r, int scene, uint8_t* rgb8);
 Status trace_rays(Renderer& r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t, cudaStream_t s,
                   bool brute);
 Status trace_count(Renderer& r, const float* d_rays, uint32_t n, uint64_t* visits, uint64_t* tests);
+// Closest hit (or brute force) of n device rays against the scene d_scene;
+// d_ctrl receives the device status word.  Synchronises `s`.
+Status launch_trace_closest(const SceneDev* d_scene, WaveCtrl* d_ctrl, const float* d_rays, uint32_t n,
+                            int32_t* d_prim, float* d_t, cudaStream_t s, int sm_count, bool brute);
 
 // error string per thread (api.cu)
 void set_last_error(const Status& s);

@@ -832,24 +832,28 @@ Status renderer_get_ppm(Renderer& r, int scene, uint8_t* rgb8) {
   return Status();
 }
 
-Status trace_rays(Renderer& r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t, cudaStream_t s,
-                  bool brute) {
-  if (r.scenes.empty()) return Status::invalid("renderer has no scene");
+Status launch_trace_closest(const SceneDev* d_scene, WaveCtrl* d_ctrl, const float* d_rays, uint32_t n,
+                            int32_t* d_prim, float* d_t, cudaStream_t s, int sm_count, bool brute) {
   if (n == 0) return Status();
-  LISA_CUDA(cudaMemsetAsync(r.ctrl, 0, sizeof(WaveCtrl), s));
+  LISA_CUDA(cudaMemsetAsync(d_ctrl, 0, sizeof(WaveCtrl), s));
+  const uint32_t blocks = std::min<uint32_t>((n + 127) / 128, (uint32_t)sm_count * 16);
   if (brute) {
-    k_brute_rays<<<std::min<uint32_t>((n + 127) / 128, r.sm_count * 16), 128, 0, s>>>(r.d_scenes, d_rays, n, d_prim,
-                                                                                     d_t);
+    k_brute_rays<<<blocks, 128, 0, s>>>(d_scene, d_rays, n, d_prim, d_t);
   } else {
-    k_trace_rays<false><<<std::min<uint32_t>((n + 127) / 128, r.sm_count * 16), 128, 0, s>>>(r.d_scenes, d_rays, n,
-                                                                                            d_prim, d_t, r.ctrl);
+    k_trace_rays<false><<<blocks, 128, 0, s>>>(d_scene, d_rays, n, d_prim, d_t, d_ctrl);
   }
   LISA_CUDA(cudaGetLastError());
   uint32_t status = 0;
-  LISA_CUDA(cudaMemcpyAsync(&status, &r.ctrl->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  LISA_CUDA(cudaMemcpyAsync(&status, &d_ctrl->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   LISA_CUDA(cudaStreamSynchronize(s));
   if (status) return Status(LISA_ERR_DEVICE, "device status word " + std::to_string(status));
   return Status();
+}
+
+Status trace_rays(Renderer& r, const float* d_rays, uint32_t n, int32_t* d_prim, float* d_t, cudaStream_t s,
+                  bool brute) {
+  if (r.scenes.empty()) return Status::invalid("renderer has no scene");
+  return launch_trace_closest(r.d_scenes, r.ctrl, d_rays, n, d_prim, d_t, s, r.sm_count, brute);
 }
 
 Status trace_count(Renderer& r, const float* d_rays, uint32_t n, uint64_t* visits, uint64_t* tests) {
