@@ -208,7 +208,7 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   Status st;
   {
     TempDeviceBufs tmp;
-    st = build_bvh(d_v, T, r.stream, tmp, r.arena, &s.nodes, &s.tris, &s.bvh);
+    st = build_bvh(d_v, T, r.stream, tmp, r.arena, &s.nodes, &s.tris, &s.bvh, d_m);
     cudaStreamSynchronize(r.stream);
   }
   if (d_v) cudaFree(d_v);

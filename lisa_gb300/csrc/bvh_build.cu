@@ -344,6 +344,7 @@ struct CollapseArgs {
   const uint32_t* first;
   const uint32_t* last;
   const float* verts;
+  const int32_t* mats;  // material per triangle, or null
   uint4* nodes;
   float4* tris;
   uint32_t* counters;  // [0] nodes, [1] tri slots, [2] next work count
@@ -464,7 +465,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ work, uint3
         const float* t = a.verts + 9ull * prim;
         float4* o = a.tris + 3ull * (tri_base + toff + q);
         o[0] = make_float4(t[0], t[1], t[2], __int_as_float((int)prim));
-        o[1] = make_float4(t[3], t[4], t[5], 0.0f);
+        o[1] = make_float4(t[3], t[4], t[5], __int_as_float(a.mats ? a.mats[prim] : 0));
         o[2] = make_float4(t[6], t[7], t[8], 0.0f);
       }
       toff += cnt;
@@ -542,7 +543,7 @@ size_t bvh_temp_bytes(uint32_t n) {
 size_t bvh_output_bytes(uint32_t n) { return (size_t)(al256(80ull * (n + 1)) + al256(48ull * n)); }
 
 Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource& tmp, ScratchSource& out,
-                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info) {
+                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info, const int32_t* d_mat) {
   auto t0 = std::chrono::steady_clock::now();
   if (n == 0) {
     *d_nodes = nullptr;
@@ -610,7 +611,7 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource
   LISA_CUDA(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
   const uint2 root = make_uint2(0u, n > 1 ? 0u : LEAF_BIT);
   LISA_CUDA(cudaMemcpyAsync(work0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
-  CollapseArgs a{n, vals, plo, phi, ilo, ihi, left, right, first, last, d_verts, nodes, tris, counters};
+  CollapseArgs a{n, vals, plo, phi, ilo, ihi, left, right, first, last, d_verts, d_mat, nodes, tris, counters};
   uint32_t nwork = 1, depth = 0;
   uint2 *wi = work0, *wo = work1;
   while (nwork > 0) {

@@ -13,7 +13,7 @@
 //            meta[i] = count<<5 | offset (count 1..3 triangles at
 //            tri_base + offset); meta 0 and imask 0 = empty slot.
 //   tris   : 3 x float4 per leaf triangle slot, in leaf order:
-//            (v0.xyz, original triangle id as int bits), (v1, 0), (v2, 0)
+//            (v0.xyz, original triangle id as int bits), (v1, material), (v2, 0)
 //   prims  : 5 x float4 per original triangle (shading record):
 //            (v0, n0.x) (v1, n0.y) (v2, n0.z) (n1, n2.x) (n2.y, n2.z, mat, 0)
 //   mats   : DevMaterial, 48 B each
@@ -123,9 +123,12 @@ struct WaveCtrl {
 struct RayPre {
   float ox, oy, oz;
   float ix, iy, iz;  // 1/d per axis
-  int kx, ky, kz;
+  uint32_t k;        // shear axes: kx | ky << 2 | kz << 4
   float Sx, Sy, Sz;
   float slack;  // absolute slack on the best distance, in t units
+  __device__ __forceinline__ int kx() const { return (int)(k & 3u); }
+  __device__ __forceinline__ int ky() const { return (int)((k >> 2) & 3u); }
+  __device__ __forceinline__ int kz() const { return (int)((k >> 4) & 3u); }
 };
 
 __device__ __forceinline__ float sel3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
@@ -150,9 +153,7 @@ __device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
     kx = ky;
     ky = t;
   }
-  r.kx = kx;
-  r.ky = ky;
-  r.kz = kz;
+  r.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
   r.Sx = fdiv(sel3(d.x, d.y, d.z, kx), dz);
   r.Sy = fdiv(sel3(d.x, d.y, d.z, ky), dz);
   r.Sz = fdiv(1.0f, dz);
@@ -167,9 +168,10 @@ __device__ __forceinline__ float intersect_tri(const RayPre& r, float4 a4, float
   const float ax_ = fsub(a4.x, r.ox), ay_ = fsub(a4.y, r.oy), az_ = fsub(a4.z, r.oz);
   const float bx_ = fsub(b4.x, r.ox), by_ = fsub(b4.y, r.oy), bz_ = fsub(b4.z, r.oz);
   const float cx_ = fsub(c4.x, r.ox), cy_ = fsub(c4.y, r.oy), cz_ = fsub(c4.z, r.oz);
-  const float Akx = sel3(ax_, ay_, az_, r.kx), Aky = sel3(ax_, ay_, az_, r.ky), Akz = sel3(ax_, ay_, az_, r.kz);
-  const float Bkx = sel3(bx_, by_, bz_, r.kx), Bky = sel3(bx_, by_, bz_, r.ky), Bkz = sel3(bx_, by_, bz_, r.kz);
-  const float Ckx = sel3(cx_, cy_, cz_, r.kx), Cky = sel3(cx_, cy_, cz_, r.ky), Ckz = sel3(cx_, cy_, cz_, r.kz);
+  const int kx = r.kx(), ky = r.ky(), kz = r.kz();
+  const float Akx = sel3(ax_, ay_, az_, kx), Aky = sel3(ax_, ay_, az_, ky), Akz = sel3(ax_, ay_, az_, kz);
+  const float Bkx = sel3(bx_, by_, bz_, kx), Bky = sel3(bx_, by_, bz_, ky), Bkz = sel3(bx_, by_, bz_, kz);
+  const float Ckx = sel3(cx_, cy_, cz_, kx), Cky = sel3(cx_, cy_, cz_, ky), Ckz = sel3(cx_, cy_, cz_, kz);
   // shear
   const float Axs = fsub(Akx, fmul(r.Sx, Akz)), Ays = fsub(Aky, fmul(r.Sy, Akz));
   const float Bxs = fsub(Bkx, fmul(r.Sx, Bkz)), Bys = fsub(Bky, fmul(r.Sy, Bkz));
@@ -189,133 +191,186 @@ __device__ __forceinline__ float intersect_tri(const RayPre& r, float4 a4, float
 }
 
 // ---------------------------------------------------------------------------
-// Closest-hit traversal of the 8-wide compressed BVH.  Box tests are made
-// conservative by padding each slab distance by 2^-21 (|c| + 255 |s|), which
-// bounds the rounding of q*s + c with s = 2^e/d and c = (p-o)/d, so the
-// traversal never culls a box the exact ray enters.  Candidates are culled
-// against best_t*(1+2^-16) + slack.  Together with the lowest-index tie rule
-// the result equals a brute-force scan with the same triangle test.
+// Closest-hit traversal of the 8-wide compressed BVH, one node per step.
+//
+// Box tests are made conservative by padding each slab distance by
+// 2^-21 (|c| + 255 |s|), which bounds the rounding of q*s + c with
+// s = 2^e/d and c = (p-o)/d, so the traversal never culls a box the exact
+// ray enters.  Candidates are culled against best_t*(1+2^-16) + slack.
+// Together with the lowest-index tie rule the result equals a brute-force
+// scan with the same triangle test.
+//
+// The traversal is resumable: trav_step() processes one node -- its eight
+// child boxes, then, in one flat loop, the triangles of the leaf children it
+// hit -- and moves to the nearest internal child, pushing the others sorted
+// by entry distance.  Kernels call it once per loop trip, so a lane whose
+// ray finished can start another ray while the rest of its warp is still
+// traversing.
+
+struct TraceScene {
+  const uint4* nodes;
+  const float4* tris;
+  uint32_t num_nodes;
+  float extent;
+};
+
+__device__ __forceinline__ TraceScene trace_scene(const SceneDev& sc) {
+  TraceScene t;
+  t.nodes = sc.nodes;
+  t.tris = sc.tris;
+  t.num_nodes = sc.num_nodes;
+  t.extent = sc.extent;
+  return t;
+}
+
+constexpr uint32_t NODE_NONE = 0xffffffffu;
+
+struct TravState {
+  RayPre r;
+  float tmin;
+  float best_t;
+  float cull;  // best_t * (1+2^-16) + slack
+  int best_prim;
+  int best_mat;  // material of the best hit (carried by the leaf triangle)
+  uint32_t node;
+  int sp;
+};
 
 __device__ __forceinline__ float byte_f(uint32_t w, int b) { return (float)((w >> (8 * b)) & 0xffu); }
 
+// Starts a ray; returns false when there is nothing to traverse (empty
+// scene or zero direction), in which case the ray is a miss.
+__device__ __forceinline__ bool trav_begin(TravState& s, const TraceScene& sc, V3 o, V3 d, float tmin, float tmax) {
+  s.best_t = tmax;
+  s.cull = tmax;
+  s.best_prim = -1;
+  s.tmin = tmin;
+  s.sp = 0;
+  s.node = 0;
+  if (sc.num_nodes == 0 || is_zero(d)) return false;
+  s.r = ray_prepare(o, d, sc.extent);
+  return true;
+}
+
+// Processes one node.  Returns true when the traversal is finished
+// (s.best_prim / s.best_t hold the result, best_prim -1 on a miss).
 template <bool COUNT>
-__device__ __forceinline__ void closest_hit(const SceneDev& sc, V3 o, V3 d, float tmin, float tmax, int& out_prim,
-                                            float& out_t, uint32_t& visits, uint32_t& tests, uint32_t* status) {
-  out_prim = -1;
-  out_t = __int_as_float(0x7f800000);
-  if (sc.num_nodes == 0 || is_zero(d)) return;
-  const RayPre r = ray_prepare(o, d, sc.extent);
-  float best_t = tmax;
-  int best_prim = -1;  // hits need t < tmax until the first one is found
-  float cull = tmax;   // best_t * (1+2^-16) + slack (tmax itself is exact)
+__device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, uint2* stack, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* status) {
+  const RayPre& r = s.r;
+  if (COUNT) ++visits;
+  const uint4* np = sc.nodes + 5ull * s.node;
+  const uint4 n0 = __ldg(np + 0);
+  const uint4 n1 = __ldg(np + 1);
+  const uint4 n2 = __ldg(np + 2);
+  const uint4 n3 = __ldg(np + 3);
+  const uint4 n4 = __ldg(np + 4);
+  const float sx = __int_as_float((n0.w & 0xffu) << 23) * r.ix;
+  const float sy = __int_as_float(((n0.w >> 8) & 0xffu) << 23) * r.iy;
+  const float sz = __int_as_float(((n0.w >> 16) & 0xffu) << 23) * r.iz;
+  const float cx = (__uint_as_float(n0.x) - r.ox) * r.ix;
+  const float cy = (__uint_as_float(n0.y) - r.oy) * r.iy;
+  const float cz = (__uint_as_float(n0.z) - r.oz) * r.iz;
+  const float gx = 4.76837158203125e-7f * (fabsf(cx) + 255.0f * fabsf(sx));
+  const float gy = 4.76837158203125e-7f * (fabsf(cy) + 255.0f * fabsf(sy));
+  const float gz = 4.76837158203125e-7f * (fabsf(cz) + 255.0f * fabsf(sz));
+  const float cnx = cx - gx, cfx = cx + gx;
+  const float cny = cy - gy, cfy = cy + gy;
+  const float cnz = cz - gz, cfz = cz + gz;
   const bool negx = r.ix < 0.0f, negy = r.iy < 0.0f, negz = r.iz < 0.0f;
-
-  uint2 stack[TRAV_STACK];
-  int sp = 0;
-  uint32_t node = 0;
-  while (true) {
-    if (COUNT) ++visits;
-    const uint4* np = sc.nodes + 5ull * node;
-    const uint4 n0 = __ldg(np + 0);
-    const uint4 n1 = __ldg(np + 1);
-    const uint4 n2 = __ldg(np + 2);
-    const uint4 n3 = __ldg(np + 3);
-    const uint4 n4 = __ldg(np + 4);
-    const float sx = __int_as_float((n0.w & 0xffu) << 23) * r.ix;
-    const float sy = __int_as_float(((n0.w >> 8) & 0xffu) << 23) * r.iy;
-    const float sz = __int_as_float(((n0.w >> 16) & 0xffu) << 23) * r.iz;
-    const float cx = (__uint_as_float(n0.x) - r.ox) * r.ix;
-    const float cy = (__uint_as_float(n0.y) - r.oy) * r.iy;
-    const float cz = (__uint_as_float(n0.z) - r.oz) * r.iz;
-    const float gx = 4.76837158203125e-7f * (fabsf(cx) + 255.0f * fabsf(sx));
-    const float gy = 4.76837158203125e-7f * (fabsf(cy) + 255.0f * fabsf(sy));
-    const float gz = 4.76837158203125e-7f * (fabsf(cz) + 255.0f * fabsf(sz));
-    const float cnx = cx - gx, cfx = cx + gx;
-    const float cny = cy - gy, cfy = cy + gy;
-    const float cnz = cz - gz, cfz = cz + gz;
-    // near/far quantised planes per axis
-    const uint32_t qlx0 = n2.x, qlx1 = n2.y, qly0 = n2.z, qly1 = n2.w;
-    const uint32_t qlz0 = n3.x, qlz1 = n3.y, qhx0 = n3.z, qhx1 = n3.w;
-    const uint32_t qhy0 = n4.x, qhy1 = n4.y, qhz0 = n4.z, qhz1 = n4.w;
-    const uint32_t nx0 = negx ? qhx0 : qlx0, nx1 = negx ? qhx1 : qlx1, fx0 = negx ? qlx0 : qhx0, fx1 = negx ? qlx1 : qhx1;
-    const uint32_t ny0 = negy ? qhy0 : qly0, ny1 = negy ? qhy1 : qly1, fy0 = negy ? qly0 : qhy0, fy1 = negy ? qly1 : qhy1;
-    const uint32_t nz0 = negz ? qhz0 : qlz0, nz1 = negz ? qhz1 : qlz1, fz0 = negz ? qlz0 : qhz0, fz1 = negz ? qlz1 : qhz1;
-    const uint32_t imask = n0.w >> 24;
-    const uint32_t child_base = n1.x, tri_base = n1.y;
-
-    uint32_t next = 0xffffffffu;
-    float next_t = 0.0f;
+  const uint32_t nx0 = negx ? n3.z : n2.x, nx1 = negx ? n3.w : n2.y;
+  const uint32_t fx0 = negx ? n2.x : n3.z, fx1 = negx ? n2.y : n3.w;
+  const uint32_t ny0 = negy ? n4.x : n2.z, ny1 = negy ? n4.y : n2.w;
+  const uint32_t fy0 = negy ? n2.z : n4.x, fy1 = negy ? n2.w : n4.y;
+  const uint32_t nz0 = negz ? n4.z : n3.x, nz1 = negz ? n4.w : n3.y;
+  const uint32_t fz0 = negz ? n3.x : n4.z, fz1 = negz ? n3.y : n4.w;
+  const uint32_t imask = n0.w >> 24;
+  const uint32_t child_base = n1.x, tri_base = n1.y;
+  // child boxes: hit mask; internal children that are hit go straight onto
+  // the stack with their entry distance (predicated stores, no branches)
+  uint32_t hit = 0;
+  const int sp0 = s.sp;
+  int sp = sp0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xffu;
-      const bool internal = (imask >> c) & 1u;
-      if (!internal && meta == 0) continue;
-      const int b = c & 3;
-      const float tnx = fmaf(byte_f(c < 4 ? nx0 : nx1, b), sx, cnx);
-      const float tny = fmaf(byte_f(c < 4 ? ny0 : ny1, b), sy, cny);
-      const float tnz = fmaf(byte_f(c < 4 ? nz0 : nz1, b), sz, cnz);
-      const float tfx = fmaf(byte_f(c < 4 ? fx0 : fx1, b), sx, cfx);
-      const float tfy = fmaf(byte_f(c < 4 ? fy0 : fy1, b), sy, cfy);
-      const float tfz = fmaf(byte_f(c < 4 ? fz0 : fz1, b), sz, cfz);
-      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-      const float tf = fminf(fminf(tfx, tfy), fminf(tfz, cull));
-      if (!(tn <= tf)) continue;
-      if (internal) {
-        const uint32_t child = child_base + meta;
-        if (next == 0xffffffffu) {
-          next = child;
-          next_t = tn;
-        } else {
-          uint32_t push = child;
-          float push_t = tn;
-          if (tn < next_t) {
-            push = next;
-            push_t = next_t;
-            next = child;
-            next_t = tn;
-          }
-          if (sp < TRAV_STACK) {
-            stack[sp++] = make_uint2(push, __float_as_uint(push_t));
-          } else if (status) {
-            atomicOr(status, ST_STACK_OVERFLOW);
-          }
-        }
-      } else {
-        const uint32_t cnt = meta >> 5, off = meta & 31u;
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const float4* tp = sc.tris + 3ull * (tri_base + off + k);
-          const float4 a = __ldg(tp + 0), bb = __ldg(tp + 1), cc = __ldg(tp + 2);
-          if (COUNT) ++tests;
-          const float t = intersect_tri(r, a, bb, cc, tmin);
-          const int prim = __float_as_int(a.w);
-          if (t < best_t || (t == best_t && prim < best_prim)) {
-            best_t = t;
-            best_prim = prim;
-            cull = fmaf(best_t, 1.52587890625e-5f, best_t) + r.slack;
-          }
-        }
-      }
+  for (int c = 0; c < 8; ++c) {
+    const int b = c & 3;
+    const float a0 = fmaf(byte_f(c < 4 ? nx0 : nx1, b), sx, cnx);
+    const float a1 = fmaf(byte_f(c < 4 ? ny0 : ny1, b), sy, cny);
+    const float a2 = fmaf(byte_f(c < 4 ? nz0 : nz1, b), sz, cnz);
+    const float f0 = fmaf(byte_f(c < 4 ? fx0 : fx1, b), sx, cfx);
+    const float f1 = fmaf(byte_f(c < 4 ? fy0 : fy1, b), sy, cfy);
+    const float f2 = fmaf(byte_f(c < 4 ? fz0 : fz1, b), sz, cfz);
+    const float tn = fmaxf(fmaxf(a0, a1), fmaxf(a2, s.tmin));
+    const float tf = fminf(fminf(f0, f1), fminf(f2, s.cull));
+    const bool h = tn <= tf;
+    hit |= (h ? 1u : 0u) << c;
+    if (h && ((imask >> c) & 1u) && sp < TRAV_STACK) {
+      const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * b)) & 0xffu;
+      stack[sp++] = make_uint2(child_base + meta, __float_as_uint(tn));
     }
-    if (next != 0xffffffffu && next_t <= cull) {
-      node = next;
-      continue;
-    }
-    // pop
-    bool found = false;
-    while (sp > 0) {
-      const uint2 e = stack[--sp];
-      if (__uint_as_float(e.y) <= cull) {
-        node = e.x;
-        found = true;
-        break;
-      }
-    }
-    if (!found) break;
   }
-  if (best_prim >= 0) {
-    out_prim = best_prim;
-    out_t = best_t;
+  if (status && (imask & hit) && sp == TRAV_STACK && __popc(imask & hit) > sp - sp0) atomicOr(status, ST_STACK_OVERFLOW);
+  // occupied slots: internal children and leaves with a non-zero meta byte
+  uint32_t leafmask = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) leafmask |= ((((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xe0u) ? 1u : 0u) << c;
+  leafmask &= ~imask & hit;
+  // triangles of the hit leaves, as a bitmask over the node's triangle slots
+  uint32_t tmask = 0;
+  while (leafmask) {
+    const int c = __ffs(leafmask) - 1;
+    leafmask &= leafmask - 1;
+    const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xffu;
+    tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
   }
+  while (tmask) {
+    const int j = __ffs(tmask) - 1;
+    tmask &= tmask - 1;
+    const float4* tp = sc.tris + 3ull * (tri_base + (uint32_t)j);
+    const float4 a = __ldg(tp + 0), bb = __ldg(tp + 1), cc = __ldg(tp + 2);
+    if (COUNT) ++tests;
+    const float t = intersect_tri(r, a, bb, cc, s.tmin);
+    const int prim = __float_as_int(a.w);
+    if (t < s.best_t || (t == s.best_t && prim < s.best_prim)) {
+      s.best_t = t;
+      s.best_prim = prim;
+      s.best_mat = __float_as_int(bb.w);
+      s.cull = fmaf(t, 1.52587890625e-5f, t) + r.slack;
+    }
+  }
+  // order the children just pushed by entry distance, nearest on top
+  // (entry distances are positive, so their bit patterns order as floats)
+  for (int i = sp0 + 1; i < sp; ++i) {
+    const uint2 e = stack[i];
+    int k = i;
+    while (k > sp0 && stack[k - 1].y < e.y) {
+      stack[k] = stack[k - 1];
+      --k;
+    }
+    stack[k] = e;
+  }
+  s.sp = sp;
+  while (s.sp > 0) {
+    const uint2 e = stack[--s.sp];
+    if (__uint_as_float(e.y) <= s.cull) {
+      s.node = e.x;
+      return false;
+    }
+  }
+  return true;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void closest_hit(const TraceScene& sc, V3 o, V3 d, float tmin, float tmax, int& out_prim,
+                                            float& out_t, uint32_t& visits, uint32_t& tests, uint32_t* status) {
+  TravState s;
+  uint2 stack[TRAV_STACK];
+  if (trav_begin(s, sc, o, d, tmin, tmax)) {
+    while (!trav_step<COUNT>(s, sc, stack, visits, tests, status)) {
+    }
+  }
+  out_prim = s.best_prim;
+  out_t = s.best_prim >= 0 ? s.best_t : __int_as_float(0x7f800000);
 }
 
 // Brute-force scan in original triangle order with the same test and tie

@@ -104,9 +104,11 @@ struct BvhBuildResult {
 
 // Builds the 8-wide compressed BVH of `num_prims` triangles whose vertices
 // are d_verts (3 float3 per triangle, device).  Temporaries come from `tmp`,
-// the node and leaf-triangle arrays from `out`.
+// the node and leaf-triangle arrays from `out`.  With d_mat (one material
+// index per triangle, device) each leaf triangle also carries its material.
 Status build_bvh(const float* d_verts, uint32_t num_prims, cudaStream_t stream, ScratchSource& tmp,
-                 ScratchSource& out, uint4** d_nodes, float4** d_tris, BvhBuildResult* info);
+                 ScratchSource& out, uint4** d_nodes, float4** d_tris, BvhBuildResult* info,
+                 const int32_t* d_mat = nullptr);
 // Device bytes build_bvh takes from `tmp` and from `out` for n triangles.
 size_t bvh_temp_bytes(uint32_t n);
 size_t bvh_output_bytes(uint32_t n);

@@ -33,6 +33,13 @@ namespace lisa {
 
 constexpr uint32_t FULL = 0xffffffffu;
 
+#ifndef LISA_NEE_MIN_BLOCKS
+#define LISA_NEE_MIN_BLOCKS 7  // 7 x 128 threads per SM (72 registers)
+#endif
+#ifndef LISA_REFILL_IDLE
+#define LISA_REFILL_IDLE 12  // idle lanes (of 32) that trigger a refill round
+#endif
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -148,7 +155,8 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
 }
 
 // ---------------------------------------------------------------------------
-// closest hit of the queued rays
+// closest hit of the queued rays: each lane traverses one node per loop trip
+// and takes the next ray as soon as its own is done (warp-aggregated fetch).
 
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
@@ -164,21 +172,40 @@ __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
     if (depth > 0) b.ctrl->rays_bounce += count;
   }
   const int lane = threadIdx.x & 31;
-  uint32_t visits = 0, tests = 0;
+  const uint32_t lt = lanemask_lt();
+  uint2 stack[TRAV_STACK];
+  TravState s;
+  TraceScene ts;
+  uint32_t ray = 0, visits = 0, tests = 0;
+  bool active = false, exhausted = false;
   while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&b.ctrl->head[HEAD_TRACE], 32u);
-    base = __shfl_sync(FULL, base, 0);
-    if (base >= count) break;
-    const uint32_t i = base + lane;
-    if (i < count) {
-      const float4 o = b.ro[q][i], d = b.rd[q][i];
-      const uint32_t slot = __float_as_uint(o.w);
-      const uint32_t scene = __float_as_uint(b.ps_col[slot].w) >> 24;
-      int prim;
-      float t;
-      closest_hit<COUNT>(b.scenes[scene], ld3(o), ld3(d), RAY_TMIN, d.w, prim, t, visits, tests, &b.ctrl->status);
-      b.hit[i] = make_int2(prim, __float_as_int(t));
+    // take new rays only once enough lanes are idle (see k_nee)
+    if (__popc(__ballot_sync(FULL, active)) <= 32 - LISA_REFILL_IDLE) {
+      const bool need = !active && !exhausted;
+      const uint32_t nmask = __ballot_sync(FULL, need);
+      if (nmask) {
+        const int leader = __ffs(nmask) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&b.ctrl->head[HEAD_TRACE], (uint32_t)__popc(nmask));
+        base = __shfl_sync(FULL, base, leader);
+        if (need) {
+          ray = base + __popc(nmask & lt);
+          if (ray < count) {
+            const float4 o = b.ro[q][ray], d = b.rd[q][ray];
+            const uint32_t slot = __float_as_uint(o.w);
+            ts = trace_scene(b.scenes[__float_as_uint(b.ps_col[slot].w) >> 24]);
+            active = trav_begin(s, ts, ld3(o), ld3(d), RAY_TMIN, d.w);
+            if (!active) b.hit[ray] = make_int2(-1, 0x7f800000);
+          } else {
+            exhausted = true;
+          }
+        }
+      }
+      if (!__any_sync(FULL, active || !exhausted)) break;
+    }
+    if (active && trav_step<COUNT>(s, ts, stack, visits, tests, &b.ctrl->status)) {
+      b.hit[ray] = make_int2(s.best_prim, s.best_prim >= 0 ? __float_as_int(s.best_t) : 0x7f800000);
+      active = false;
     }
   }
   if (COUNT) {
@@ -276,97 +303,115 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
 // ---------------------------------------------------------------------------
 // emitter search + bounce (shader.cu:196-209, 248-253; lambertian.cu:7-22)
 //
-// Each lane owns one opaque vertex and casts one shadow ray per loop trip;
-// a lane whose vertex finished takes the next one (warp-aggregated refill),
-// so warps stay full while vertices need between 1 and 30 rays.
+// Each lane owns one opaque vertex at a time and runs a small state machine:
+// start a shadow ray (hemisphere draw), traverse one BVH node per loop trip,
+// and when the ray ends apply the reference's occlusion programs; after an
+// emitter is seen (or 30 rays) it draws the bounce, writes the path state,
+// appends the continuation ray and takes the next vertex.  Lanes advance
+// independently, so a warp stays full while its vertices need between 1 and
+// 30 rays of different lengths.
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_nee(WaveBufs b, int depth) {
+__global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->nee_count;
   const int lane = threadIdx.x & 31;
   const uint32_t lt = lanemask_lt();
-  bool have = false, exhausted = false;
-  uint32_t slot = 0, tries = 0, seed = 0;
-  int stale = -1, mat_idx = 0;
+  uint2 stack[TRAV_STACK];
+  TravState s;
+  TraceScene ts;
   const SceneDev* sc = nullptr;
-  V3 p = v3(0.0f), N = v3(0.0f), D = v3(0.0f), att = v3(0.0f), col = v3(0.0f);
-  float colw = 0.0f;
+  bool have = false, exhausted = false, ray_active = false;
+  uint32_t entry = 0, slot = 0, tries = 0, seed = 0;
+  int stale = -1, mat_idx = 0;
+  // the vertex position lives in the shadow ray's origin (s.r.o*)
+  V3 N = v3(0.0f), dir = v3(0.0f);
+  s.r.ox = s.r.oy = s.r.oz = 0.0f;
   uint32_t shadow = 0, visits = 0, tests = 0;
+  bool pending = false;  // a finished shadow ray not yet evaluated
   while (true) {
-    const bool need = !have && !exhausted;
-    const uint32_t nmask = __ballot_sync(FULL, need);
-    if (nmask) {
-      const int leader = __ffs(nmask) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(&b.ctrl->head[HEAD_NEE], (uint32_t)__popc(nmask));
-      base = __shfl_sync(FULL, base, leader);
-      if (need) {
-        const uint32_t idx = base + __popc(nmask & lt);
-        if (idx < count) {
-          const float4 a4 = b.nee_a[idx], b4 = b.nee_b[idx], c4 = b.nee_c[idx];
-          p = ld3(a4);
-          slot = __float_as_uint(a4.w);
-          N = ld3(b4);
-          mat_idx = __float_as_int(b4.w);
-          D = ld3(c4);
-          const float4 at = b.ps_att[slot];
-          att = ld3(at);
-          stale = __float_as_int(at.w);
-          const float4 c = b.ps_col[slot];
-          col = ld3(c);
-          colw = c.w;
-          sc = b.scenes + (__float_as_uint(c.w) >> 24);
-          seed = b.ps_rng[slot];
-          tries = 0;
-          have = true;
+    // Bookkeeping (evaluate finished rays, finish and fetch vertices, start
+    // rays) runs only once enough lanes are idle, so its divergent code is
+    // shared by many lanes; otherwise the warp keeps traversing.
+    const uint32_t busy = __ballot_sync(FULL, ray_active);
+    if (__popc(busy) <= 32 - LISA_REFILL_IDLE) {
+      bool want_ray = false;
+      V3 nd = v3(0.0f);
+      if (pending) {
+        pending = false;
+        if (s.best_prim >= 0) {
+          // the occlusion hit program marks a hit only on an emitter and
+          // otherwise leaves the flag as it was (shader.cu:177-184)
+          const int hm = s.best_mat;
+          if (sc->mats[hm].cls == MAT_EMIT) stale = hm;
         } else {
-          exhausted = true;
+          stale = -1;  // miss (shader.cu:172-175)
+        }
+        const bool lit = stale >= 0;
+        if (lit || ++tries == (uint32_t)NEE_TRIES) {
+          const float4 at = b.ps_att[slot];
+          const V3 att = ld3(at);
+          if (lit) {
+            const DevMaterial& em = sc->mats[stale];
+            const float brdf = bsdf::BRDF(N, dir, sc->mats[mat_idx]);
+            const float4 c = b.ps_col[slot];
+            const V3 col = ld3(c) + (v3(em.emission[0], em.emission[1], em.emission[2]) * brdf) * att;
+            b.ps_col[slot] = make_float4(col.x, col.y, col.z, c.w);
+          }
+          // the bounce is drawn at every vertex, the last one included, so
+          // the per-pixel stream advances exactly as in the reference
+          const V3 D = ld3(b.nee_c[entry]);
+          nd = bsdf::bounce(D, N, seed, sc->mats[mat_idx]);
+          want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
+          b.ps_rng[slot] = seed;
+          b.ps_att[slot] = make_float4(att.x, att.y, att.z, __int_as_float(stale));
+          have = false;
         }
       }
-    }
-    if (!__any_sync(FULL, have)) break;
-    bool finish = false;
-    if (have) {
-      const V3 dir = bsdf::shoot_ray_hemisphere(N, seed);
-      int hp;
-      float ht;
-      closest_hit<COUNT>(*sc, p, dir, RAY_TMIN, RAY_TMAX, hp, ht, visits, tests, &b.ctrl->status);
-      ++shadow;
-      if (hp >= 0) {
-        // the occlusion hit program marks a hit only on an emitter and
-        // otherwise leaves the flag as it was (shader.cu:177-184)
-        const int hm = prim_material(*sc, hp);
-        if (sc->mats[hm].cls == MAT_EMIT) stale = hm;
-      } else {
-        stale = -1;  // miss (shader.cu:172-175)
+      const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
+      if (want_ray) {
+        b.ro[q ^ 1][ri] = make_float4(s.r.ox, s.r.oy, s.r.oz, __uint_as_float(slot));
+        b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
       }
-      if (stale >= 0) {
-        const DevMaterial& em = sc->mats[stale];
-        const DevMaterial& me = sc->mats[mat_idx];
-        const float brdf = bsdf::BRDF(N, dir, me);
-        col = col + (v3(em.emission[0], em.emission[1], em.emission[2]) * brdf) * att;
-        finish = true;
-      } else if (++tries == (uint32_t)NEE_TRIES) {
-        finish = true;
+      const bool need = !have && !exhausted;
+      const uint32_t nmask = __ballot_sync(FULL, need);
+      if (nmask) {
+        const int leader = __ffs(nmask) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&b.ctrl->head[HEAD_NEE], (uint32_t)__popc(nmask));
+        base = __shfl_sync(FULL, base, leader);
+        if (need) {
+          entry = base + __popc(nmask & lt);
+          if (entry < count) {
+            const float4 a4 = b.nee_a[entry], b4 = b.nee_b[entry];
+            s.r.ox = a4.x;
+            s.r.oy = a4.y;
+            s.r.oz = a4.z;
+            slot = __float_as_uint(a4.w);
+            N = ld3(b4);
+            mat_idx = __float_as_int(b4.w);
+            stale = __float_as_int(b.ps_att[slot].w);
+            seed = b.ps_rng[slot];
+            sc = b.scenes + (__float_as_uint(b.ps_col[slot].w) >> 24);
+            ts = trace_scene(*sc);
+            tries = 0;
+            have = true;
+          } else {
+            exhausted = true;
+          }
+        }
+      }
+      if (!__any_sync(FULL, have)) break;
+      if (have && !ray_active && !pending) {
+        dir = bsdf::shoot_ray_hemisphere(N, seed);
+        ++shadow;
+        ray_active = trav_begin(s, ts, v3(s.r.ox, s.r.oy, s.r.oz), dir, RAY_TMIN, RAY_TMAX);
+        pending = !ray_active;  // nothing to traverse: a miss
       }
     }
-    bool want_ray = false;
-    V3 nd = v3(0.0f);
-    if (finish) {
-      // the bounce is drawn at every vertex, the last one included, so the
-      // per-pixel stream advances exactly as in the reference
-      nd = bsdf::bounce(D, N, seed, sc->mats[mat_idx]);
-      want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
-      b.ps_rng[slot] = seed;
-      b.ps_att[slot] = make_float4(att.x, att.y, att.z, __int_as_float(stale));
-      b.ps_col[slot] = make_float4(col.x, col.y, col.z, colw);
-      have = false;
-    }
-    const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
-    if (want_ray) {
-      b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
-      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+    if (ray_active && trav_step<COUNT>(s, ts, stack, visits, tests, &b.ctrl->status)) {
+      ray_active = false;
+      pending = true;
     }
   }
   warp_add64(&b.ctrl->rays_shadow, shadow);
@@ -486,8 +531,8 @@ __global__ void __launch_bounds__(128) k_trace_rays(const SceneDev* __restrict__
       const float* r = rays + 8ull * i;
       int hp;
       float ht;
-      closest_hit<COUNT>(*scd, v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7], hp, ht, visits, tests,
-                         &ctrl->status);
+      closest_hit<COUNT>(trace_scene(*scd), v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7], hp, ht, visits,
+                         tests, &ctrl->status);
       if (prim) prim[i] = hp;
       if (tout) tout[i] = ht;
     }
