@@ -323,6 +323,11 @@ def run_ours(args, rank, ws, local):
             "stages_ms_per_step": {"trace": trace_ms / args.steps, "shade": shade_ms / args.steps,
                                    "nee": nee_ms / args.steps, "other": other_ms / args.steps},
             "rays_per_step": rays / args.steps,
+            "traversal_per_ray": {
+                "shadow": {"nodes": cs.node_visits_nee / max(cs.rays_shadow, 1),
+                           "tris": cs.tri_tests_nee / max(cs.rays_shadow, 1)},
+                "radiance": {"nodes": cs.node_visits_trace / max(cs.rays_primary + cs.rays_bounce, 1),
+                             "tris": cs.tri_tests_trace / max(cs.rays_primary + cs.rays_bounce, 1)}},
             "wall_s": wall,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),

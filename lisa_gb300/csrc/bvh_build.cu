@@ -99,6 +99,15 @@ __device__ __forceinline__ uint32_t expand10(uint32_t v) {
   return v;
 }
 
+#ifndef LISA_MORTON_SIZE_BITS
+#define LISA_MORTON_SIZE_BITS 2
+#endif
+
+// Sort key: the triangle's size class above the 30-bit Morton code of its
+// centroid (extended Morton codes, Vinkler, Bittner, Havran, HPG 2017), so
+// large triangles -- walls, quads -- separate from the small ones near the
+// root instead of overlapping every deep subtree.  Class 0 holds triangles
+// whose box diagonal exceeds 1/8 of the scene's, then 1/64, 1/512.
 __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict__ hi, uint32_t n,
                          const int* __restrict__ bounds, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -114,7 +123,20 @@ __global__ void k_morton(const float4* __restrict__ lo, const float4* __restrict
     u = fminf(fmaxf(u, 0.0f), 1.0f);
     q[k] = min((uint32_t)(u * 1024.0f), 1023u);
   }
-  keys[i] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+  uint32_t key = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+#if LISA_MORTON_SIZE_BITS > 0
+  float s2 = 0.0f, t2 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float se = ord2f(bounds[3 + k]) - ord2f(bounds[k]);
+    s2 += se * se;
+  }
+  t2 = (b.x - a.x) * (b.x - a.x) + (b.y - a.y) * (b.y - a.y) + (b.z - a.z) * (b.z - a.z);
+  // diagonal ratio thresholds 1/8, 1/64, 1/512 on squared lengths
+  const uint32_t cls = t2 * 64.0f > s2 ? 0u : (t2 * 4096.0f > s2 ? 1u : (t2 * 262144.0f > s2 ? 2u : 3u));
+  key |= cls << 30;
+#endif
+  keys[i] = key;
   vals[i] = i;
 }
 

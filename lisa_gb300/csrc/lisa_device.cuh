@@ -138,9 +138,10 @@ __device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
   r.ox = o.x;
   r.oy = o.y;
   r.oz = o.z;
-  r.ix = fdiv(1.0f, d.x);
-  r.iy = fdiv(1.0f, d.y);
-  r.iz = fdiv(1.0f, d.z);
+  // __frcp_rn is the correctly rounded 1/x, the same value as 1.0f/x
+  r.ix = __frcp_rn(d.x);
+  r.iy = __frcp_rn(d.y);
+  r.iz = __frcp_rn(d.z);
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
   int kx = kz + 1;
@@ -156,9 +157,9 @@ __device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
   r.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
   r.Sx = fdiv(sel3(d.x, d.y, d.z, kx), dz);
   r.Sy = fdiv(sel3(d.x, d.y, d.z, ky), dz);
-  r.Sz = fdiv(1.0f, dz);
-  const float dmax = fmaxf(ax, fmaxf(ay, az));
-  r.slack = 3.814697265625e-6f * extent / dmax;  // 2^-18 * extent / |d|max
+  r.Sz = __frcp_rn(dz);
+  // 2^-18 * extent / |d|max; a margin, so an approximate quotient will do
+  r.slack = __fdividef(3.814697265625e-6f * extent, fmaxf(ax, fmaxf(ay, az)));
   return r;
 }
 
