@@ -92,6 +92,7 @@ Status BumpScratch::get(void** p, size_t bytes, const char* what) {
 Renderer::~Renderer() {
   if (stream) cudaStreamSynchronize(stream);
   for (auto e : ev_pool) cudaEventDestroy(e);
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (d_waves) cudaFree(d_waves);
   guides.clear();
   arena.release_all();

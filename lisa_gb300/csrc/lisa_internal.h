@@ -176,6 +176,12 @@ struct Renderer {
   int shade_blocks = 0, shade_threads = 256;
   // events for stage timing
   std::vector<cudaEvent_t> ev_pool;
+  // CUDA graph of the last launch sequence, reused while its shape (waves
+  // and their depths, flags, wave-table address) stays the same
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<uint64_t> graph_key;
+  std::vector<std::pair<int, std::pair<size_t, size_t>>> graph_marks;
+  uint32_t graph_launches[4] = {0, 0, 0, 0};
   // guided mode
   std::vector<std::unique_ptr<GuideNet>> guides;
   void* guide_bufs = nullptr;

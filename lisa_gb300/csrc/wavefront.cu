@@ -651,6 +651,7 @@ WaveBufs make_bufs(Renderer& r) {
 struct StageTimer {
   Renderer& r;
   bool on;
+  bool capturing = false;  // inside stream capture: record external event nodes
   size_t next = 0;
   std::vector<std::pair<int, std::pair<size_t, size_t>>> marks;  // stage, (start ev, end ev)
   explicit StageTimer(Renderer& rr, bool enable) : r(rr), on(enable) {}
@@ -661,7 +662,10 @@ struct StageTimer {
       r.ev_pool.push_back(e);
     }
     *idx = next++;
-    LISA_CUDA(cudaEventRecord(r.ev_pool[*idx], r.stream));
+    if (capturing)
+      LISA_CUDA(cudaEventRecordWithFlags(r.ev_pool[*idx], r.stream, cudaEventRecordExternal));
+    else
+      LISA_CUDA(cudaEventRecord(r.ev_pool[*idx], r.stream));
     return Status();
   }
 };
@@ -747,9 +751,65 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   LISA_CUDA(cudaEventCreate(&e1));
   LISA_CUDA(cudaEventRecord(e0, r.stream));
   StageTimer tm(r, r.opts.stage_timing != 0);
-  Status s = launch_wave_sequence(r, wb, &local, &tm);
+  Status s;
+  if (r.opts.use_graph && !wb.empty()) {
+    // one graph per launch-sequence shape; the wave table it reads is
+    // refreshed above, outside the graph
+    std::vector<uint64_t> key(wb.begin(), wb.end());
+    key.push_back(r.opts.count_traversal);
+    key.push_back(r.opts.stage_timing);
+    key.push_back((uint64_t)(uintptr_t)r.d_waves);
+    if (key != r.graph_key || !r.graph_exec) {
+      if (tm.on) {  // create the timing events before capture begins
+        size_t need = 0;
+        for (uint32_t d : wb) need += 2ull * (3ull * d + 2);
+        while (r.ev_pool.size() < need) {
+          cudaEvent_t e;
+          LISA_CUDA(cudaEventCreate(&e));
+          r.ev_pool.push_back(e);
+        }
+      }
+      if (r.graph_exec) cudaGraphExecDestroy(r.graph_exec);
+      r.graph_exec = nullptr;
+      r.graph_key.clear();
+      cudaGraph_t g = nullptr;
+      LISA_CUDA(cudaStreamBeginCapture(r.stream, cudaStreamCaptureModeThreadLocal));
+      lisa_render_stats counts;
+      std::memset(&counts, 0, sizeof(counts));
+      tm.capturing = true;
+      s = launch_wave_sequence(r, wb, &counts, &tm);
+      tm.capturing = false;
+      const cudaError_t ce = cudaStreamEndCapture(r.stream, &g);
+      if (s.ok() && ce != cudaSuccess) s = Status::cuda(ce, "cudaStreamEndCapture");
+      if (s.ok()) {
+        const cudaError_t ie = cudaGraphInstantiate(&r.graph_exec, g, 0);
+        if (ie != cudaSuccess) s = Status::cuda(ie, "cudaGraphInstantiate");
+      }
+      if (g) cudaGraphDestroy(g);
+      if (s.ok()) {
+        r.graph_key = key;
+        r.graph_marks = tm.marks;
+        r.graph_launches[0] = counts.launches_trace;
+        r.graph_launches[1] = counts.launches_shade;
+        r.graph_launches[2] = counts.launches_nee;
+        r.graph_launches[3] = counts.launches_total;
+      }
+    }
+    if (s.ok()) {
+      tm.marks = r.graph_marks;
+      local.launches_trace = r.graph_launches[0];
+      local.launches_shade = r.graph_launches[1];
+      local.launches_nee = r.graph_launches[2];
+      local.launches_total = r.graph_launches[3];
+      const cudaError_t le = cudaGraphLaunch(r.graph_exec, r.stream);
+      if (le != cudaSuccess) s = Status::cuda(le, "cudaGraphLaunch");
+    }
+  } else {
+    s = launch_wave_sequence(r, wb, &local, &tm);
+  }
   LISA_CUDA(cudaEventRecord(e1, r.stream));
   if (!s.ok()) {
+    cudaStreamSynchronize(r.stream);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return s;

@@ -113,6 +113,20 @@ def test_batch_of_uneven_scenes_matches_single_renders(gpu):
         assert np.array_equal(batch.image(k), single.image()), k
 
 
+def test_cuda_graph_replay_matches_stream_launches(gpu):
+    """The captured graph (reused across calls with the same wave shape,
+    fresh wave table each call) gives the same image as direct launches."""
+    sc = scenes.cornell_box(width=32, height=24, num_samples=3, num_bounces=5)
+    a = L.Renderer(L.params_from_scene(sc), use_graph=0, stage_timing=1)
+    b = L.Renderer(L.params_from_scene(sc), use_graph=1, stage_timing=1)
+    for _ in range(3):
+        sa = a.render_progressive(3)
+        sb = b.render_progressive(3)
+        assert sa.rays == sb.rays and sb.launches_total == sa.launches_total
+        assert sb.ms_nee > 0 and sb.ms_trace > 0
+    assert np.array_equal(a.image(), b.image())
+
+
 def test_wave_splitting_small_capacity(gpu):
     """A capacity smaller than one image plane splits planes into pixel
     ranges; the result is unchanged."""
