@@ -1,24 +1,724 @@
-// MLP path guide (placeholder until the tensor-core kernels land).
+// MLP path guide: fused tcgen05 kernels for inference, training (forward,
+// loss gradient, backward) and Adam.
+//
+// Network: 64 encoded inputs -> 4 x (64, ReLU) -> 40 outputs = 8 vMF lobes
+// (guide_mix.cuh).  FP32 master weights; BF16 copies, pre-swizzled into the
+// K-major 128-byte-swizzle layout the UMMA descriptors expect, are copied
+// once per CTA into shared memory.  A CTA of 128 threads processes tiles of
+// 128 samples: thread t owns row t of every activation tile, and TMEM lane
+// t of every accumulator.  One elected thread issues tcgen05.mma (M = 128,
+// K = 16 per instruction) and commits to an mbarrier; waits are bounded and
+// a time-out sets a status bit instead of hanging.
+//
+// Backward of layer l (weights W_l: out x in):
+//   dH_{l-1} = dZ_l W_l          A = dZ_l tile [b][o] (K = o), B = W_l^T rows
+//   dW_l    += dZ_l^T H_{l-1}    A = [dZ_l^T ; H_{l-1}^T] (M = 128, K = batch),
+//                                B = H_{l-1}^T; rows 0..63 of D are dW_l
+// dW accumulates in TMEM across all tiles of the CTA and is added to the
+// global FP32 gradient once at the end.
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
 #include "guide.cuh"
+#include "guide_mix.cuh"
+#include "lisa_device.cuh"
+#include "tcgen05.cuh"
 
 namespace lisa {
 
-GuideNet::~GuideNet() {}
+// ---- parameter layout (FP32 master) ------------------------------------------
+constexpr int P_W = 0;                    // W1..W4: 4 x 64 x 64, then W5: 40 x 64
+constexpr int P_W5 = 4 * 64 * 64;
+constexpr int P_B = P_W5 + 40 * 64;       // b1..b4: 4 x 64, then b5: 40
+constexpr int P_B5 = P_B + 4 * 64;
+constexpr int NPARAM = P_B5 + 40;
+static_assert(NPARAM == LISA_GUIDE_NUM_PARAMS, "parameter count");
 
-Status guide_renderer_init(Renderer&) { return Status(LISA_ERR_UNSUPPORTED, "guided mode not built yet"); }
+// ---- packed BF16 weights: rows of 128 B, pre-swizzled in 8-row groups ------------
+constexpr int R_FWD = 0;        // W1..W4 forward: 4 x 64 rows (row = output)
+constexpr int R_W5 = 256;       // W5 forward: 48 rows (40 used)
+constexpr int R_T = 304;        // W2^T..W5^T: 4 x 64 rows (row = input, K = output)
+constexpr int R_TOTAL = 560;
+constexpr int PACK_BYTES = R_TOTAL * 128;
+constexpr int FWD_BYTES = R_T * 128;  // what inference needs
+
+__device__ __forceinline__ uint16_t f2bf(float x) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+__device__ __forceinline__ float bf2f(uint16_t h) { return __bfloat162float(__ushort_as_bfloat16(h)); }
+
+// master -> packed BF16 (forward and transposed copies)
+__global__ void k_guide_pack(const float* __restrict__ master, uint16_t* __restrict__ pack) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // one element of the 560 x 64 image
+  if (e >= R_TOTAL * 64) return;
+  const int row = e >> 6, k = e & 63;
+  float v = 0.0f;
+  if (row < R_W5) {
+    const int l = row >> 6, o = row & 63;
+    v = master[P_W + l * 4096 + o * 64 + k];
+  } else if (row < R_T) {
+    const int o = row - R_W5;
+    v = o < 40 ? master[P_W5 + o * 64 + k] : 0.0f;
+  } else {
+    const int l = 1 + ((row - R_T) >> 6);  // W2..W5 (0-based layer 1..4)
+    const int i = (row - R_T) & 63, o = k;
+    if (l < 4) v = master[P_W + l * 4096 + o * 64 + i];
+    else v = o < 40 ? master[P_W5 + o * 64 + i] : 0.0f;
+  }
+  uint8_t* base = (uint8_t*)pack + (size_t)(row & ~7) * 128;
+  *(uint16_t*)(base + tc::sw128_offset(row & 7, k)) = f2bf(v);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters.
+__global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
+                             const float* __restrict__ g, float lr, float b1c, float b2c, uint32_t* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NPARAM) return;
+  const float gi = g[i];
+  if (!isfinite(gi)) {
+    atomicOr(status, ST_GUIDE_NONFINITE);
+    return;
+  }
+  const float mi = 0.9f * m[i] + 0.1f * gi;
+  const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  master[i] -= lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
+}
+
+// ---- sample sources -------------------------------------------------------------
+// RAW: n x 64 FP32 features.  GEOM: 16 floats per sample (position, normal,
+// view, direction, weight) encoded against the scene box.  NEE: the
+// renderer's emitter-search queue (position, normal, incoming direction).
+enum { SRC_RAW = 0, SRC_GEOM = 1, SRC_NEE = 2 };
+
+struct GuideSrc {
+  const float* raw;       // SRC_RAW features
+  const float* dirs;      // SRC_RAW directions (n x 3) for training
+  const float* weights;   // SRC_RAW weights (n) for training
+  const float4* geom;     // SRC_GEOM: 4 float4 per sample
+  const float4* nee_a;    // SRC_NEE: hit point
+  const float4* nee_b;    // SRC_NEE: normal
+  const float4* nee_c;    // SRC_NEE: incoming direction
+  const uint32_t* count;  // device sample count (SRC_NEE / SRC_GEOM), else null
+  uint32_t n;             // host sample count when count == null
+  float bmin[3], bmax[3];
+};
+
+template <int SRC>
+__device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, float* f) {
+  if (SRC == SRC_RAW) {
+    const float4* r = (const float4*)(s.raw + 64ull * i);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const float4 x = __ldg(r + c);
+      f[4 * c] = x.x;
+      f[4 * c + 1] = x.y;
+      f[4 * c + 2] = x.z;
+      f[4 * c + 3] = x.w;
+    }
+  } else if (SRC == SRC_GEOM) {
+    const float4 a = s.geom[4ull * i], b = s.geom[4ull * i + 1], c = s.geom[4ull * i + 2];
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, f);
+  } else {
+    const float4 a = s.nee_a[i], b = s.nee_b[i], c = s.nee_c[i];
+    // view direction: towards where the ray came from
+    const float il = rsqrtf(fmaxf(c.x * c.x + c.y * c.y + c.z * c.z, 1e-30f));
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il, f);
+  }
+}
+
+// Writes 64 values as BF16 into row `row` of a swizzled tile.
+__device__ __forceinline__ void store_row_bf16(uint8_t* tile, int row, const float* v) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    uint4 q;
+    q.x = (uint32_t)f2bf(v[8 * c + 0]) | ((uint32_t)f2bf(v[8 * c + 1]) << 16);
+    q.y = (uint32_t)f2bf(v[8 * c + 2]) | ((uint32_t)f2bf(v[8 * c + 3]) << 16);
+    q.z = (uint32_t)f2bf(v[8 * c + 4]) | ((uint32_t)f2bf(v[8 * c + 5]) << 16);
+    q.w = (uint32_t)f2bf(v[8 * c + 6]) | ((uint32_t)f2bf(v[8 * c + 7]) << 16);
+    *(uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4)) = q;
+  }
+}
+
+__device__ __forceinline__ void load_row_bf16(const uint8_t* tile, int row, float* v) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const uint4 q = *(const uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4));
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      v[8 * c + 2 * j] = bf2f((uint16_t)(w[j] & 0xffffu));
+      v[8 * c + 2 * j + 1] = bf2f((uint16_t)(w[j] >> 16));
+    }
+  }
+}
+
+// D = A(128 x 64) * B(N x 64)^T: four K = 16 steps, then a commit.
+__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* a, const uint8_t* b, uint32_t N,
+                                            uint64_t* mbar) {
+  const uint32_t sa = tc::smem_u32(a), sb = tc::smem_u32(b);
+  const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) tc::mma_bf16(d_tmem, tc::sw128_desc(sa + 32 * k), tc::sw128_desc(sb + 32 * k), idesc, k);
+  tc::mma_commit(mbar);
+}
+
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  return (uint8_t*)(((uintptr_t)p + 1023) & ~(uintptr_t)1023);
+}
+
+// ---------------------------------------------------------------------------------
+// inference: out[i][0..39] = network(features_i)
+
+// + 1024 for the manual 1024-byte alignment, + 16 KB of slack after the last
+// operand tile
+constexpr int INFER_SMEM = FWD_BYTES + 2 * 16384 + 1024 + 16384;
+
+template <int SRC>
+__global__ void __launch_bounds__(128, 1) k_guide_infer(const uint16_t* __restrict__ pack, const float* __restrict__ master,
+                                                        GuideSrc src, float* __restrict__ out, uint32_t* status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* w = smem;
+  uint8_t* act[2] = {smem + FWD_BYTES, smem + FWD_BYTES + 16384};
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int failed;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t n = src.count ? *(volatile const uint32_t*)src.count : src.n;
+  const uint32_t ntiles = (n + 127) / 128;
+  if (blockIdx.x >= ntiles) return;
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    failed = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+  for (int c = tid; c < FWD_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
+  tc::fence_smem_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t i = t * 128 + tid;
+    float f[64];
+    if (i < n) load_features<SRC>(src, i, f);
+    else
+#pragma unroll
+      for (int k = 0; k < 64; ++k) f[k] = 0.0f;
+    store_row_bf16(act[0], tid, f);
+    int cur = 0;
+    for (int l = 0; l < 5; ++l) {
+      tc::fence_smem_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      const uint32_t N = l < 4 ? 64u : 48u;
+      if (tid == 0) issue_layer(tmem, act[cur], w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, N, &mbar);
+      if (!tc::mbar_wait(&mbar, phase)) {
+        atomicOr(status, ST_GUIDE_NONFINITE << 1);
+        failed = 1;
+      }
+      phase ^= 1;
+      tc::fence_after_sync();
+      __syncthreads();
+      if (failed) break;
+      float acc[64];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (c * 16 < (int)N) tc::tmem_ld16(lane_addr + c * 16, acc + c * 16);
+      }
+      if (l < 4) {
+        const float* b = master + P_B + 64 * l;
+#pragma unroll
+        for (int k = 0; k < 64; ++k) acc[k] = fmaxf(acc[k] + __ldg(b + k), 0.0f);
+        store_row_bf16(act[cur ^ 1], tid, acc);
+        cur ^= 1;
+      } else if (i < n) {
+        float4* o = (float4*)(out + 40ull * i);
+#pragma unroll
+        for (int k = 0; k < 10; ++k)
+          o[k] = make_float4(acc[4 * k] + __ldg(master + P_B5 + 4 * k), acc[4 * k + 1] + __ldg(master + P_B5 + 4 * k + 1),
+                             acc[4 * k + 2] + __ldg(master + P_B5 + 4 * k + 2),
+                             acc[4 * k + 3] + __ldg(master + P_B5 + 4 * k + 3));
+      }
+      tc::fence_before_sync();
+    }
+    if (failed) break;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+// ---------------------------------------------------------------------------------
+// training: grads += d loss / d params, loss += sum of the per-sample losses
+
+constexpr int TILE = 16384;
+constexpr int TRAIN_OFF_ACT = PACK_BYTES;              // X, H1..H4
+constexpr int TRAIN_OFF_DZ = TRAIN_OFF_ACT + 5 * TILE;  // dZ tile [b][o]
+constexpr int TRAIN_OFF_AT = TRAIN_OFF_DZ + TILE;       // [dZ^T ; H^T], two K halves
+constexpr int TRAIN_SMEM_USED = TRAIN_OFF_AT + 2 * TILE;
+constexpr int TRAIN_SMEM = TRAIN_SMEM_USED + 1024 + 16384;
+static_assert(TRAIN_SMEM <= 227 * 1024, "training kernel shared memory");
+constexpr uint32_t TM_FWD = 0, TM_DH = 64, TM_DW = 128;  // TMEM columns; dW_l at 128 + 64 l
+
+// element (m, b) of the transposed operand: two K halves of [128 x 64]
+__device__ __forceinline__ uint32_t at_offset(uint32_t m, uint32_t b) {
+  return (b >> 6) * (uint32_t)TILE + tc::sw128_offset(m, b & 63u);
+}
+
+__device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int count) {
+  // column sums over the block: warp shuffle reduction, then shared atomics
+  for (int k = 0; k < count; ++k) {
+    float x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s_db[k], x);
+  }
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restrict__ pack, const float* __restrict__ master,
+                                                        GuideSrc src, float inv_n, float* __restrict__ grads,
+                                                        float* __restrict__ loss_out, uint32_t* status) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* w = smem;
+  uint8_t* act = smem + TRAIN_OFF_ACT;  // tile l = H_l (H_0 = X)
+  uint8_t* dzt = smem + TRAIN_OFF_DZ;
+  uint8_t* at = smem + TRAIN_OFF_AT;
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int failed;
+  __shared__ float s_db[4 * 64 + 40];
+  __shared__ float s_loss;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t n = src.count ? *(volatile const uint32_t*)src.count : src.n;
+  const uint32_t ntiles = (n + 127) / 128;
+  if (blockIdx.x >= ntiles) return;
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    failed = 0;
+    s_loss = 0.0f;
+  }
+  for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
+  for (int c = tid; c < PACK_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
+  tc::fence_smem_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  uint32_t phase = 0;
+  bool first = true;
+  auto wait_mma = [&]() {
+    if (!tc::mbar_wait(&mbar, phase)) {
+      atomicOr(status, ST_GUIDE_NONFINITE << 1);
+      failed = 1;
+    }
+    phase ^= 1;
+    tc::fence_after_sync();
+    __syncthreads();
+  };
+  auto sync_for_mma = [&]() {
+    tc::fence_smem_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  };
+  for (uint32_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
+    const uint32_t i = t * 128 + tid;
+    const bool valid = i < n;
+    float v[64];
+    float wx = 0.0f, wy = 0.0f, wz = 1.0f, wt = 0.0f;
+    if (valid) {
+      load_features<SRC>(src, i, v);
+      if (SRC == SRC_RAW) {
+        wx = __ldg(src.dirs + 3ull * i);
+        wy = __ldg(src.dirs + 3ull * i + 1);
+        wz = __ldg(src.dirs + 3ull * i + 2);
+        wt = __ldg(src.weights + i);
+      } else {
+        const float4 c = src.geom[4ull * i + 2], d = src.geom[4ull * i + 3];
+        wx = c.y;
+        wy = c.z;
+        wz = c.w;
+        wt = d.x;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 64; ++k) v[k] = 0.0f;
+    }
+    store_row_bf16(act, tid, v);
+    // forward
+    for (int l = 0; l < 5 && !failed; ++l) {
+      sync_for_mma();
+      const uint32_t N = l < 4 ? 64u : 48u;
+      if (tid == 0) issue_layer(tmem + TM_FWD, act + l * TILE, w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, N, &mbar);
+      wait_mma();
+      if (failed) break;
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (c * 16 < (int)N) tc::tmem_ld16(tmem + TM_FWD + lane_off + c * 16, v + c * 16);
+      if (l < 4) {
+#pragma unroll
+        for (int k = 0; k < 64; ++k) v[k] = fmaxf(v[k] + __ldg(master + P_B + 64 * l + k), 0.0f);
+        store_row_bf16(act + (l + 1) * TILE, tid, v);
+      }
+      tc::fence_before_sync();
+    }
+    if (failed) break;
+    // loss gradient at the output (40 values, padded with zeros to 64)
+    float g[64];
+    {
+      float o[40];
+#pragma unroll
+      for (int k = 0; k < 40; ++k) o[k] = v[k] + __ldg(master + P_B5 + k);
+      float lsum = 0.0f;
+      if (valid && wt != 0.0f) {
+        const float il = rsqrtf(fmaxf(wx * wx + wy * wy + wz * wz, 1e-30f));
+        lsum = guide::loss_grad(o, wx * il, wy * il, wz * il, wt * inv_n, g);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 40; ++k) g[k] = 0.0f;
+      }
+#pragma unroll
+      for (int k = 40; k < 64; ++k) g[k] = 0.0f;
+#pragma unroll
+      for (int o2 = 16; o2 > 0; o2 >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o2);
+      if ((tid & 31) == 0) atomicAdd(&s_loss, lsum);
+    }
+    add_bias_grad(s_db + 4 * 64, g, 40);
+    // backward, layer 5 (index 4) down to layer 1 (index 0)
+    for (int l = 4; l >= 0 && !failed; --l) {
+      // dZ_l (registers g) -> dZ tile (A of dH) and dZ^T rows of AT;
+      // H_{l-1} (tile l) -> H^T rows of AT
+      store_row_bf16(dzt, tid, g);
+      {
+        float h[64];
+        load_row_bf16(act + l * TILE, tid, h);
+#pragma unroll 8
+        for (int k = 0; k < 64; ++k) {
+          *(uint16_t*)(at + at_offset((uint32_t)k, (uint32_t)tid)) = f2bf(g[k]);
+          *(uint16_t*)(at + at_offset((uint32_t)(64 + k), (uint32_t)tid)) = f2bf(h[k]);
+        }
+      }
+      sync_for_mma();
+      if (tid == 0) {
+        // dW_l += [dZ^T ; H^T] x (H^T)^T over the 128 samples (K = 128)
+        const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
+        const uint32_t sat = tc::smem_u32(at);
+#pragma unroll
+        for (uint32_t ks = 0; ks < 8; ++ks) {
+          const uint32_t base = sat + (ks >> 2) * TILE + (ks & 3) * 32;
+          tc::mma_bf16(tmem + TM_DW + 64 * l, tc::sw128_desc(base), tc::sw128_desc(base + 64 * 128), idesc,
+                       (first && ks == 0) ? 0u : 1u);
+        }
+        if (l > 0) {
+          // dH_{l-1} = dZ_l W_l  (B = W_l^T rows)
+          const uint32_t sdz = tc::smem_u32(dzt), swt = tc::smem_u32(w + (R_T + 64 * (l - 1)) * 128);
+#pragma unroll
+          for (uint32_t k = 0; k < 4; ++k)
+            tc::mma_bf16(tmem + TM_DH, tc::sw128_desc(sdz + 32 * k), tc::sw128_desc(swt + 32 * k), idesc, k);
+        }
+        tc::mma_commit(&mbar);
+      }
+      wait_mma();
+      if (failed) break;
+      if (l > 0) {
+        float h[64];
+        load_row_bf16(act + l * TILE, tid, h);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DH + lane_off + c * 16, g + c * 16);
+#pragma unroll
+        for (int k = 0; k < 64; ++k) g[k] = h[k] > 0.0f ? g[k] : 0.0f;
+        add_bias_grad(s_db + 64 * (l - 1), g, 64);
+      }
+      tc::fence_before_sync();
+    }
+    first = false;
+  }
+  // flush: dW rows 0..63 live in TMEM lanes of warps 0 and 1
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (!failed && !first && warp < 2) {
+    const int o = warp * 32 + (tid & 31);
+    for (int l = 0; l < 5; ++l) {
+      const int rows = l < 4 ? 64 : 40;
+      float d[64];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DW + 64 * l + lane_off + c * 16, d + c * 16);
+      if (o < rows) {
+        float* gw = grads + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64;
+        for (int k = 0; k < 64; ++k) atomicAdd(gw + k, d[k]);
+      }
+    }
+  }
+  __syncthreads();
+  if (!failed && !first) {
+    for (int k = tid; k < 4 * 64 + 40; k += 128) atomicAdd(grads + P_B + k, s_db[k]);
+    if (tid == 0) atomicAdd(loss_out, s_loss);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------------
+// host
+
+GuideNet::~GuideNet() {
+  if (master) cudaFree(master);
+  if (adam_m) cudaFree(adam_m);
+  if (adam_v) cudaFree(adam_v);
+  if (grads) cudaFree(grads);
+  if (w_bf16) cudaFree(w_bf16);
+  if (loss) cudaFree(loss);
+  if (status) cudaFree(status);
+}
+
+namespace {
+
+Status guide_alloc(GuideNet& g) {
+  LISA_CUDA(cudaMalloc(&g.master, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMalloc(&g.adam_m, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMalloc(&g.adam_v, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMalloc(&g.grads, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMalloc(&g.w_bf16, PACK_BYTES));
+  LISA_CUDA(cudaMalloc(&g.loss, sizeof(float)));
+  LISA_CUDA(cudaMalloc(&g.status, sizeof(uint32_t)));
+  LISA_CUDA(cudaMemset(g.adam_m, 0, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMemset(g.adam_v, 0, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMemset(g.grads, 0, sizeof(float) * NPARAM));
+  LISA_CUDA(cudaMemset(g.loss, 0, sizeof(float)));
+  LISA_CUDA(cudaMemset(g.status, 0, sizeof(uint32_t)));
+  return Status();
+}
+
+// He-uniform weights (ReLU layers), small output layer, zero biases; the
+// kappa logits start at log(2).
+std::vector<float> guide_init(uint32_t seed) {
+  std::vector<float> p(NPARAM, 0.0f);
+  std::mt19937 gen(seed * 2654435761u + 12345u);
+  const float a = std::sqrt(6.0f / 64.0f);
+  std::uniform_real_distribution<float> U(-a, a), U5(-0.1f, 0.1f);
+  for (int i = 0; i < 4 * 4096; ++i) p[P_W + i] = U(gen);
+  for (int i = 0; i < 40 * 64; ++i) p[P_W5 + i] = U5(gen);
+  for (int k = 0; k < 8; ++k) p[P_B5 + 5 * k + 3] = std::log(2.0f);
+  return p;
+}
+
+}  // namespace
+
+Status guide_pack(GuideNet& g, cudaStream_t s) {
+  k_guide_pack<<<(R_TOTAL * 64 + 255) / 256, 256, 0, s>>>(g.master, g.w_bf16);
+  LISA_CUDA(cudaGetLastError());
+  return Status();
+}
+
+Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s) {
+  std::unique_ptr<GuideNet> g(new GuideNet());
+  LISA_TRY(guide_alloc(*g));
+  std::vector<float> p = guide_init(seed);
+  LISA_CUDA(cudaMemcpyAsync(g->master, p.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice, s));
+  LISA_TRY(guide_pack(*g, s));
+  LISA_CUDA(cudaStreamSynchronize(s));
+  static bool attr_set = false;
+  if (!attr_set) {
+    LISA_CUDA(cudaFuncSetAttribute(k_guide_train<SRC_RAW>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM));
+    LISA_CUDA(cudaFuncSetAttribute(k_guide_train<SRC_GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM));
+    LISA_CUDA(cudaFuncSetAttribute(k_guide_infer<SRC_RAW>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM));
+    LISA_CUDA(cudaFuncSetAttribute(k_guide_infer<SRC_NEE>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM));
+    attr_set = true;
+  }
+  out = std::move(g);
+  return Status();
+}
+
+static int sm_count_current() {
+  int dev = 0, sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  return sm > 0 ? sm : 1;
+}
+
+Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n, cudaStream_t s) {
+  const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
+  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
+  if (src_kind == SRC_RAW)
+    k_guide_infer<SRC_RAW><<<grid, 128, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
+  else
+    k_guide_infer<SRC_NEE><<<grid, 128, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
+  LISA_CUDA(cudaGetLastError());
+  return Status();
+}
+
+Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
+                          cudaStream_t s) {
+  LISA_CUDA(cudaMemsetAsync(g.grads, 0, sizeof(float) * NPARAM, s));
+  LISA_CUDA(cudaMemsetAsync(g.loss, 0, sizeof(float), s));
+  const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
+  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
+  if (src_kind == SRC_RAW)
+    k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status);
+  else
+    k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status);
+  LISA_CUDA(cudaGetLastError());
+  return Status();
+}
+
+Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
+  g.step++;
+  const float b1c = 1.0f - std::pow(0.9f, (float)g.step), b2c = 1.0f - std::pow(0.999f, (float)g.step);
+  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grads, lr, b1c, b2c, g.status);
+  LISA_CUDA(cudaGetLastError());
+  return guide_pack(g, s);
+}
+
+Status guide_check_status(GuideNet& g, cudaStream_t s) {
+  uint32_t st = 0;
+  LISA_CUDA(cudaMemcpyAsync(&st, g.status, sizeof(st), cudaMemcpyDeviceToHost, s));
+  LISA_CUDA(cudaStreamSynchronize(s));
+  if (st & (ST_GUIDE_NONFINITE << 1)) return Status(LISA_ERR_DEVICE, "guide: tensor-core wait timed out");
+  if (st & ST_GUIDE_NONFINITE) return Status(LISA_ERR_DEVICE, "guide: non-finite gradient");
+  return Status();
+}
+
+Status guide_renderer_init(Renderer&) { return Status(LISA_ERR_UNSUPPORTED, "guided rendering not wired yet"); }
 
 }  // namespace lisa
 
+// ===========================================================================
 using namespace lisa;
+
+struct lisa_guide {
+  std::unique_ptr<GuideNet> net;
+  cudaStream_t stream = nullptr;
+  bool owned = true;
+};
+
+static int gret(const Status& s) {
+  set_last_error(s);
+  return s.code;
+}
+
 extern "C" {
-struct lisa_guide {};
-int lisa_guide_create(uint32_t, lisa_guide**) { return LISA_ERR_UNSUPPORTED; }
-void lisa_guide_destroy(lisa_guide*) {}
-int lisa_guide_get_params(lisa_guide*, float*) { return LISA_ERR_UNSUPPORTED; }
-int lisa_guide_set_params(lisa_guide*, const float*) { return LISA_ERR_UNSUPPORTED; }
-int lisa_guide_forward(lisa_guide*, const float*, uint32_t, float*) { return LISA_ERR_UNSUPPORTED; }
-int lisa_guide_train_step(lisa_guide*, const float*, const float*, const float*, uint32_t, float, float*, float*) {
-  return LISA_ERR_UNSUPPORTED;
+
+int lisa_guide_create(uint32_t seed, lisa_guide** out) {
+  try {
+    if (!out) return gret(Status::invalid("null argument"));
+    std::unique_ptr<lisa_guide> g(new lisa_guide());
+    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return gret(Status(LISA_ERR_UNSUPPORTED, std::string("no CUDA device: ") + cudaGetErrorString(e)));
+    }
+    Status s = guide_create(seed, g->net, g->stream);
+    if (!s.ok()) return gret(s);
+    *out = g.release();
+    return gret(Status());
+  } catch (const std::exception& e) {
+    return gret(Status(LISA_ERR_INVALID, e.what()));
+  }
 }
-int lisa_renderer_guide(lisa_renderer*, int32_t, lisa_guide**) { return LISA_ERR_UNSUPPORTED; }
+
+void lisa_guide_destroy(lisa_guide* g) {
+  if (!g || !g->owned) return;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  g->net.reset();
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
 }
+
+int lisa_guide_get_params(lisa_guide* g, float* params) {
+  if (!g || !params) return gret(Status::invalid("null argument"));
+  cudaError_t e = cudaMemcpyAsync(params, g->net->master, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  return gret(e == cudaSuccess ? Status() : Status::cuda(e, "get params"));
+}
+
+int lisa_guide_set_params(lisa_guide* g, const float* params) {
+  if (!g || !params) return gret(Status::invalid("null argument"));
+  cudaError_t e = cudaMemcpyAsync(g->net->master, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice, g->stream);
+  if (e != cudaSuccess) return gret(Status::cuda(e, "set params"));
+  Status s = guide_pack(*g->net, g->stream);
+  if (s.ok()) {
+    e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) s = Status::cuda(e, "set params");
+  }
+  return gret(s);
+}
+
+int lisa_guide_forward(lisa_guide* g, const float* features, uint32_t n, float* out) {
+  if (!g || (n && (!features || !out))) return gret(Status::invalid("null argument"));
+  if (n == 0) return gret(Status());
+  float *d_x = nullptr, *d_o = nullptr;
+  auto run = [&]() -> Status {
+    LISA_CUDA(cudaMalloc(&d_x, sizeof(float) * 64ull * n));
+    LISA_CUDA(cudaMalloc(&d_o, sizeof(float) * 40ull * n));
+    LISA_CUDA(cudaMemcpyAsync(d_x, features, sizeof(float) * 64ull * n, cudaMemcpyHostToDevice, g->stream));
+    GuideSrc src;
+    std::memset(&src, 0, sizeof(src));
+    src.raw = d_x;
+    src.n = n;
+    LISA_TRY(guide_launch_infer(*g->net, src, SRC_RAW, d_o, n, g->stream));
+    LISA_CUDA(cudaMemcpyAsync(out, d_o, sizeof(float) * 40ull * n, cudaMemcpyDeviceToHost, g->stream));
+    return guide_check_status(*g->net, g->stream);
+  };
+  Status s = run();
+  if (d_x) cudaFree(d_x);
+  if (d_o) cudaFree(d_o);
+  return gret(s);
+}
+
+int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dirs, const float* weights, uint32_t n,
+                          float lr, float* loss, float* grads) {
+  if (!g || (n && (!features || !dirs || !weights))) return gret(Status::invalid("null argument"));
+  if (n == 0) return gret(Status::invalid("empty batch"));
+  float *d_x = nullptr, *d_d = nullptr, *d_w = nullptr;
+  auto run = [&]() -> Status {
+    LISA_CUDA(cudaMalloc(&d_x, sizeof(float) * 64ull * n));
+    LISA_CUDA(cudaMalloc(&d_d, sizeof(float) * 3ull * n));
+    LISA_CUDA(cudaMalloc(&d_w, sizeof(float) * n));
+    LISA_CUDA(cudaMemcpyAsync(d_x, features, sizeof(float) * 64ull * n, cudaMemcpyHostToDevice, g->stream));
+    LISA_CUDA(cudaMemcpyAsync(d_d, dirs, sizeof(float) * 3ull * n, cudaMemcpyHostToDevice, g->stream));
+    LISA_CUDA(cudaMemcpyAsync(d_w, weights, sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
+    GuideSrc src;
+    std::memset(&src, 0, sizeof(src));
+    src.raw = d_x;
+    src.dirs = d_d;
+    src.weights = d_w;
+    src.n = n;
+    LISA_TRY(guide_launch_train(*g->net, src, SRC_RAW, 1.0f / (float)n, n, g->stream));
+    if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->net->loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    if (grads)
+      LISA_CUDA(cudaMemcpyAsync(grads, g->net->grads, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream));
+    LISA_TRY(guide_check_status(*g->net, g->stream));
+    if (lr > 0.0f) {
+      LISA_TRY(guide_launch_adam(*g->net, lr, g->stream));
+      LISA_TRY(guide_check_status(*g->net, g->stream));
+    }
+    return Status();
+  };
+  Status s = run();
+  if (d_x) cudaFree(d_x);
+  if (d_d) cudaFree(d_d);
+  if (d_w) cudaFree(d_w);
+  return gret(s);
+}
+
+int lisa_renderer_guide(lisa_renderer*, int32_t, lisa_guide**) {
+  return gret(Status(LISA_ERR_UNSUPPORTED, "renderer has no guide (not in guided mode)"));
+}
+
+}  // extern "C"

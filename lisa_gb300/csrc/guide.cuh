@@ -1,7 +1,10 @@
 // MLP path guide: interfaces shared with the renderer.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <stdint.h>
+
+#include <memory>
 
 #include "lisa_internal.h"
 #include "wavefront.cuh"
@@ -16,7 +19,8 @@ struct GuideNet {
   float* adam_v = nullptr;
   float* grads = nullptr;
   uint16_t* w_bf16 = nullptr;
-  float* loss = nullptr;  // device scalar accumulator
+  float* loss = nullptr;      // device scalar accumulator
+  uint32_t* status = nullptr; // device status word (time-outs, non-finite values)
   uint32_t step = 0;
   ~GuideNet();
 };
