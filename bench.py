@@ -229,8 +229,12 @@ def run_ours(args, rank, ws, local):
 
     sc = make_scene(res=args.res)
     params = L.params_from_scene(sc)
-    opts = L.default_options(stage_timing=1, seed=1000 * rank, paths_in_flight=args.paths)
+    # each rank renders its own range of sample indices of the frame
+    # (lisa_gb300.shard); one rank renders samples 0, 1, 2, ...
+    shard_first = rank * (1 << 20)
+    opts = L.default_options(stage_timing=1, paths_in_flight=args.paths)
     r = L.Renderer(params, opts)
+    r.set_sample_offset(shard_first)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def step():
@@ -263,8 +267,9 @@ def run_ours(args, rank, ws, local):
     other_ms = sum(s.ms_other for s in stats)
     launches = sum(s.launches_total for s in stats)
     # counting pass (same seeds, one step) for the algorithmic bytes per launch
-    copts = L.default_options(seed=1000 * rank, paths_in_flight=args.paths, count_traversal=1)
+    copts = L.default_options(paths_in_flight=args.paths, count_traversal=1)
     rc = L.Renderer(params, copts)
+    rc.set_sample_offset(shard_first)
     cs = rc.render_progressive(args.spp_per_step)
     nee_bytes_step = (cs.nee_vertices * NEE_B_VERTEX + cs.rays_shadow * NEE_B_RAY +
                       cs.node_visits_nee * B_NODE + cs.tri_tests_nee * B_TRI)
@@ -288,7 +293,8 @@ def run_ours(args, rank, ws, local):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         p2 = L.params_from_arrays(v, n, mi, mats, sc.width, sc.height, sc.eye, sc.look_at, sc.fov, 256, 8)
-        r2 = L.Renderer(p2, L.default_options(seed=1000 * rank + 7 + i, paths_in_flight=args.paths))
+        r2 = L.Renderer(p2, L.default_options(paths_in_flight=args.paths))
+        r2.set_sample_offset(shard_first + (i + 1) * 4096)
         s2 = r2.render_progressive(args.spp_per_step)
         img = r2.image()
         r2.close()

@@ -110,7 +110,11 @@ typedef struct lisa_options {
   uint64_t alloc_cap_bytes;  /* refuse device allocations beyond this (0=none) */
   uint32_t count_traversal;  /* run the counting variants of the traversal
                                 kernels (node visits / triangle tests)        */
-  uint32_t reserved0;
+  uint32_t guide_warmup_waves;/* first waves train the guide but sample the
+                                BSDF only                                      */
+  uint32_t guide_steps_per_wave;/* Adam steps per wave, each on its own slice
+                                of guide_train_batch samples (0 = 1)           */
+  uint32_t reserved1;
 } lisa_options;
 
 /* Per-call statistics.  Ray counts are rays actually traced: primary +
@@ -202,6 +206,12 @@ int lisa_render(lisa_renderer* r, lisa_render_stats* stats);
 int lisa_render_progressive(lisa_renderer* r, uint32_t spp, lisa_render_stats* stats);
 /* Forget the accumulated samples (and, in guided mode, keep the guide). */
 int lisa_reset_accumulation(lisa_renderer* r);
+/* Index of the next sample of scene `scene` (LISA_RNG_PER_SAMPLE streams are
+ * keyed by it).  Renderers given disjoint sample ranges of one frame -- the
+ * shards of a multi-GPU render -- produce means that merge exactly into the
+ * single-GPU result.  No reference counterpart (the reference runs on one
+ * GPU).  Also the index lisa_reset_accumulation returns to. */
+int lisa_set_sample_offset(lisa_renderer* r, int32_t scene, uint64_t first_sample);
 
 /* Image of scene `scene` (0 for a single-scene renderer).  Any output may be
  * NULL.  rgb32: w*h*3 mean radiance, row 0 = bottom (the accum_buffer

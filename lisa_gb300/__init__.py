@@ -171,6 +171,11 @@ class Renderer:
     def reset(self):
         N.check(N.lib().lisa_reset_accumulation(self._h))
 
+    def set_sample_offset(self, first_sample: int, scene: int = 0):
+        """Render the samples first_sample, first_sample+1, ... (a shard of
+        a frame split over GPUs; see lisa_gb300.shard)."""
+        N.check(N.lib().lisa_set_sample_offset(self._h, scene, int(first_sample)))
+
     def image(self, scene: int = 0, variance: bool = False, fp64: bool = False):
         """Mean radiance (h, w, 3) float32 with row 0 = bottom; optionally the
         per-pixel sample variance (FP64) and the FP64 mean."""
@@ -243,9 +248,12 @@ class Guide:
         if handle is None:
             h = C.c_void_p()
             N.check(N.lib().lisa_guide_create(int(seed), C.byref(h)))
-            self._h, self._own = h, True
+            self._h = h
         else:
-            self._h, self._own = handle, False
+            # a renderer's network: the handle is ours to free, the network
+            # stays with the renderer (kept alive through _owner)
+            self._h = handle
+        self._own = True
 
     def params(self) -> np.ndarray:
         out = np.empty(N.GUIDE_NUM_PARAMS, np.float32)

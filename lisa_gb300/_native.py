@@ -64,7 +64,8 @@ class Options(C.Structure):
                 ("guide_bsdf_fraction", C.c_float), ("guide_lr", C.c_float),
                 ("guide_train_batch", C.c_uint32), ("guide_train_waves", C.c_uint32),
                 ("alloc_cap_bytes", C.c_uint64), ("count_traversal", C.c_uint32),
-                ("reserved0", C.c_uint32)]
+                ("guide_warmup_waves", C.c_uint32), ("guide_steps_per_wave", C.c_uint32),
+                ("reserved1", C.c_uint32)]
 
 
 class RenderStats(C.Structure):
@@ -107,6 +108,7 @@ SIGNATURES = {
     "lisa_render": (C.c_int, [_P, C.POINTER(RenderStats)]),
     "lisa_render_progressive": (C.c_int, [_P, C.c_uint32, C.POINTER(RenderStats)]),
     "lisa_reset_accumulation": (C.c_int, [_P]),
+    "lisa_set_sample_offset": (C.c_int, [_P, C.c_int32, C.c_uint64]),
     "lisa_get_image": (C.c_int, [_P, C.c_int32, _P, _P, _P, _P]),
     "lisa_get_ppm_rgb8": (C.c_int, [_P, C.c_int32, _P]),
     "lisa_save_image": (C.c_int, [_P, C.c_int32, C.c_char_p]),

@@ -512,6 +512,18 @@ int lisa_reset_accumulation(lisa_renderer* r) {
   })
 }
 
+int lisa_set_sample_offset(lisa_renderer* r, int32_t scene, uint64_t first_sample) {
+  API_GUARD({
+    if (!r) return ret(Status::invalid("null renderer"));
+    Renderer& R = *r->r;
+    if (scene < 0 || scene >= (int)R.scenes.size()) return ret(Status::invalid("scene index out of range"));
+    if (first_sample > 0xffffffffull) return ret(Status::invalid("sample index beyond 2^32"));
+    R.scenes[scene].sample_offset = first_sample;
+    R.scenes[scene].next_sample = first_sample;
+    return ret(Status());
+  })
+}
+
 int lisa_get_image(lisa_renderer* r, int32_t scene, float* rgb32, uint8_t* rgba8, double* var, double* mean64) {
   API_GUARD({
     if (!r) return ret(Status::invalid("null renderer"));
@@ -603,6 +615,21 @@ int lisa_trace_count(lisa_renderer* r, const float* rays, uint32_t n, uint64_t* 
     Status s = run();
     if (d_r) cudaFree(d_r);
     return ret(s);
+  })
+}
+
+int lisa_renderer_guide(lisa_renderer* r, int32_t scene, lisa_guide** out) {
+  API_GUARD({
+    if (!r || !out) return ret(Status::invalid("null argument"));
+    Renderer& R = *r->r;
+    if (scene < 0 || scene >= (int)R.scenes.size()) return ret(Status::invalid("scene index out of range"));
+    if (R.scenes[scene].guide < 0) return ret(Status::invalid("renderer is not in guided mode"));
+    lisa_guide* g = new lisa_guide();
+    g->borrowed = R.guides[R.scenes[scene].guide].get();
+    g->stream = R.stream;
+    g->owns_stream = false;
+    *out = g;
+    return ret(Status());
   })
 }
 

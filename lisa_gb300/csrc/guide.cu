@@ -71,11 +71,16 @@ __global__ void k_guide_pack(const float* __restrict__ master, uint16_t* __restr
   *(uint16_t*)(base + tc::sw128_offset(row & 7, k)) = f2bf(v);
 }
 
-// Adam (Kingma & Ba 2015) on the FP32 master parameters.
+// Adam (Kingma & Ba 2015) on the FP32 master parameters.  The step count
+// lives on the device (incremented by k_guide_step afterwards), so a
+// captured graph replays with the right bias correction.
 __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
-                             const float* __restrict__ g, float lr, float b1c, float b2c, uint32_t* status) {
+                             const float* __restrict__ g, float lr, const uint32_t* __restrict__ step,
+                             uint32_t* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= NPARAM) return;
+  const float t = (float)(*step + 1);
+  const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
   const float gi = g[i];
   if (!isfinite(gi)) {
     atomicOr(status, ST_GUIDE_NONFINITE);
@@ -88,24 +93,7 @@ __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, 
   master[i] -= lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
 }
 
-// ---- sample sources -------------------------------------------------------------
-// RAW: n x 64 FP32 features.  GEOM: 16 floats per sample (position, normal,
-// view, direction, weight) encoded against the scene box.  NEE: the
-// renderer's emitter-search queue (position, normal, incoming direction).
-enum { SRC_RAW = 0, SRC_GEOM = 1, SRC_NEE = 2 };
-
-struct GuideSrc {
-  const float* raw;       // SRC_RAW features
-  const float* dirs;      // SRC_RAW directions (n x 3) for training
-  const float* weights;   // SRC_RAW weights (n) for training
-  const float4* geom;     // SRC_GEOM: 4 float4 per sample
-  const float4* nee_a;    // SRC_NEE: hit point
-  const float4* nee_b;    // SRC_NEE: normal
-  const float4* nee_c;    // SRC_NEE: incoming direction
-  const uint32_t* count;  // device sample count (SRC_NEE / SRC_GEOM), else null
-  uint32_t n;             // host sample count when count == null
-  float bmin[3], bmax[3];
-};
+__global__ void k_guide_step(uint32_t* step) { *step += 1; }
 
 template <int SRC>
 __device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, float* f) {
@@ -120,13 +108,15 @@ __device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, flo
       f[4 * c + 3] = x.w;
     }
   } else if (SRC == SRC_GEOM) {
-    const float4 a = s.geom[4ull * i], b = s.geom[4ull * i + 1], c = s.geom[4ull * i + 2];
-    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, f);
+    const float4 a = s.geom[4ull * i], b = s.geom[4ull * i + 1], c = s.geom[4ull * i + 2], d = s.geom[4ull * i + 3];
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, d.y, f);
   } else {
     const float4 a = s.nee_a[i], b = s.nee_b[i], c = s.nee_c[i];
     // view direction: towards where the ray came from
     const float il = rsqrtf(fmaxf(c.x * c.x + c.y * c.y + c.z * c.z, 1e-30f));
-    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il, f);
+    const int stale = __float_as_int(s.ps_att[__float_as_uint(a.w)].w);
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il,
+                  stale >= 0 ? 1.0f : 0.0f, f);
   }
 }
 
@@ -188,8 +178,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint16_t* __restri
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const uint32_t n = src.count ? *(volatile const uint32_t*)src.count : src.n;
-  const uint32_t ntiles = (n + 127) / 128;
+  // samples [src.first, n)
+  const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
+  const uint32_t ntiles = (n - src.first + 127) / 128;
   if (blockIdx.x >= ntiles) return;
   if (tid == 0) {
     tc::mbar_init(&mbar, 1);
@@ -205,7 +196,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_infer(const uint16_t* __restri
   const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
   uint32_t phase = 0;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint32_t i = t * 128 + tid;
+    const uint32_t i = src.first + t * 128 + tid;
     float f[64];
     if (i < n) load_features<SRC>(src, i, f);
     else
@@ -300,8 +291,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   __shared__ float s_db[4 * 64 + 40];
   __shared__ float s_loss;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const uint32_t n = src.count ? *(volatile const uint32_t*)src.count : src.n;
-  const uint32_t ntiles = (n + 127) / 128;
+  // samples [src.first, n)
+  const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
+  const uint32_t ntiles = (n - src.first + 127) / 128;
   if (blockIdx.x >= ntiles) return;
   if (tid == 0) {
     tc::mbar_init(&mbar, 1);
@@ -335,7 +327,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
     tc::fence_after_sync();
   };
   for (uint32_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
-    const uint32_t i = t * 128 + tid;
+    const uint32_t i = src.first + t * 128 + tid;
     const bool valid = i < n;
     float v[64];
     float wx = 0.0f, wy = 0.0f, wz = 1.0f, wt = 0.0f;
@@ -485,6 +477,7 @@ GuideNet::~GuideNet() {
   if (w_bf16) cudaFree(w_bf16);
   if (loss) cudaFree(loss);
   if (status) cudaFree(status);
+  if (d_step) cudaFree(d_step);
 }
 
 namespace {
@@ -497,6 +490,8 @@ Status guide_alloc(GuideNet& g) {
   LISA_CUDA(cudaMalloc(&g.w_bf16, PACK_BYTES));
   LISA_CUDA(cudaMalloc(&g.loss, sizeof(float)));
   LISA_CUDA(cudaMalloc(&g.status, sizeof(uint32_t)));
+  LISA_CUDA(cudaMalloc(&g.d_step, sizeof(uint32_t)));
+  LISA_CUDA(cudaMemset(g.d_step, 0, sizeof(uint32_t)));
   LISA_CUDA(cudaMemset(g.adam_m, 0, sizeof(float) * NPARAM));
   LISA_CUDA(cudaMemset(g.adam_v, 0, sizeof(float) * NPARAM));
   LISA_CUDA(cudaMemset(g.grads, 0, sizeof(float) * NPARAM));
@@ -578,9 +573,8 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float 
 }
 
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
-  g.step++;
-  const float b1c = 1.0f - std::pow(0.9f, (float)g.step), b2c = 1.0f - std::pow(0.999f, (float)g.step);
-  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grads, lr, b1c, b2c, g.status);
+  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grads, lr, g.d_step, g.status);
+  k_guide_step<<<1, 1, 0, s>>>(g.d_step);
   LISA_CUDA(cudaGetLastError());
   return guide_pack(g, s);
 }
@@ -594,18 +588,35 @@ Status guide_check_status(GuideNet& g, cudaStream_t s) {
   return Status();
 }
 
-Status guide_renderer_init(Renderer&) { return Status(LISA_ERR_UNSUPPORTED, "guided rendering not wired yet"); }
+// Guided mode: one network per scene, the per-entry network outputs, the
+// per-slot training records and the training batch.
+Status guide_renderer_init(Renderer& r) {
+  uint32_t maxd = 1;
+  for (auto& s : r.scenes) maxd = std::max<uint32_t>(maxd, s.params.num_bounces);
+  r.max_depth = maxd;
+  const uint32_t chunk = std::max<uint32_t>(128, (r.opts.guide_train_batch + 127) / 128 * 128);
+  r.guide_chunk = chunk;
+  const uint32_t B = chunk * std::max<uint32_t>(1, r.opts.guide_steps_per_wave);
+  r.guide_batch_cap = B;
+  if (!(r.opts.guide_bsdf_fraction >= 0.0f && r.opts.guide_bsdf_fraction <= 1.0f))
+    return Status::invalid("guide_bsdf_fraction must be in [0, 1]");
+  r.guides.clear();
+  for (size_t s = 0; s < r.scenes.size(); ++s) {
+    std::unique_ptr<GuideNet> g;
+    LISA_TRY(guide_create(r.opts.seed * 7919u + (uint32_t)s, g, r.stream));
+    r.scenes[s].guide = (int)s;
+    r.guides.push_back(std::move(g));
+  }
+  LISA_TRY(r.arena.alloc((void**)&r.guide_out, sizeof(float) * 40ull * r.capacity, "guide outputs"));
+  LISA_TRY(r.arena.alloc((void**)&r.train_rec, sizeof(float4) * 5ull * maxd * r.capacity, "guide records"));
+  LISA_TRY(r.arena.alloc((void**)&r.guide_batch, sizeof(float4) * 4ull * B, "guide batch"));
+  return Status();
+}
 
 }  // namespace lisa
 
 // ===========================================================================
 using namespace lisa;
-
-struct lisa_guide {
-  std::unique_ptr<GuideNet> net;
-  cudaStream_t stream = nullptr;
-  bool owned = true;
-};
 
 static int gret(const Status& s) {
   set_last_error(s);
@@ -633,25 +644,25 @@ int lisa_guide_create(uint32_t seed, lisa_guide** out) {
 }
 
 void lisa_guide_destroy(lisa_guide* g) {
-  if (!g || !g->owned) return;
+  if (!g) return;
   if (g->stream) cudaStreamSynchronize(g->stream);
   g->net.reset();
-  if (g->stream) cudaStreamDestroy(g->stream);
+  if (g->stream && g->owns_stream) cudaStreamDestroy(g->stream);
   delete g;
 }
 
 int lisa_guide_get_params(lisa_guide* g, float* params) {
   if (!g || !params) return gret(Status::invalid("null argument"));
-  cudaError_t e = cudaMemcpyAsync(params, g->net->master, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream);
+  cudaError_t e = cudaMemcpyAsync(params, g->get().master, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
   return gret(e == cudaSuccess ? Status() : Status::cuda(e, "get params"));
 }
 
 int lisa_guide_set_params(lisa_guide* g, const float* params) {
   if (!g || !params) return gret(Status::invalid("null argument"));
-  cudaError_t e = cudaMemcpyAsync(g->net->master, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice, g->stream);
+  cudaError_t e = cudaMemcpyAsync(g->get().master, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice, g->stream);
   if (e != cudaSuccess) return gret(Status::cuda(e, "set params"));
-  Status s = guide_pack(*g->net, g->stream);
+  Status s = guide_pack(g->get(), g->stream);
   if (s.ok()) {
     e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) s = Status::cuda(e, "set params");
@@ -671,9 +682,9 @@ int lisa_guide_forward(lisa_guide* g, const float* features, uint32_t n, float* 
     std::memset(&src, 0, sizeof(src));
     src.raw = d_x;
     src.n = n;
-    LISA_TRY(guide_launch_infer(*g->net, src, SRC_RAW, d_o, n, g->stream));
+    LISA_TRY(guide_launch_infer(g->get(), src, SRC_RAW, d_o, n, g->stream));
     LISA_CUDA(cudaMemcpyAsync(out, d_o, sizeof(float) * 40ull * n, cudaMemcpyDeviceToHost, g->stream));
-    return guide_check_status(*g->net, g->stream);
+    return guide_check_status(g->get(), g->stream);
   };
   Status s = run();
   if (d_x) cudaFree(d_x);
@@ -699,14 +710,14 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
     src.dirs = d_d;
     src.weights = d_w;
     src.n = n;
-    LISA_TRY(guide_launch_train(*g->net, src, SRC_RAW, 1.0f / (float)n, n, g->stream));
-    if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->net->loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    LISA_TRY(guide_launch_train(g->get(), src, SRC_RAW, 1.0f / (float)n, n, g->stream));
+    if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->get().loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     if (grads)
-      LISA_CUDA(cudaMemcpyAsync(grads, g->net->grads, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream));
-    LISA_TRY(guide_check_status(*g->net, g->stream));
+      LISA_CUDA(cudaMemcpyAsync(grads, g->get().grads, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream));
+    LISA_TRY(guide_check_status(g->get(), g->stream));
     if (lr > 0.0f) {
-      LISA_TRY(guide_launch_adam(*g->net, lr, g->stream));
-      LISA_TRY(guide_check_status(*g->net, g->stream));
+      LISA_TRY(guide_launch_adam(g->get(), lr, g->stream));
+      LISA_TRY(guide_check_status(g->get(), g->stream));
     }
     return Status();
   };
@@ -717,8 +728,5 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
   return gret(s);
 }
 
-int lisa_renderer_guide(lisa_renderer*, int32_t, lisa_guide**) {
-  return gret(Status(LISA_ERR_UNSUPPORTED, "renderer has no guide (not in guided mode)"));
-}
 
 }  // extern "C"

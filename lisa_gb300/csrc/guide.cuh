@@ -21,10 +21,53 @@ struct GuideNet {
   uint16_t* w_bf16 = nullptr;
   float* loss = nullptr;      // device scalar accumulator
   uint32_t* status = nullptr; // device status word (time-outs, non-finite values)
-  uint32_t step = 0;
+  uint32_t* d_step = nullptr; // Adam step count (device)
   ~GuideNet();
 };
 
+// Sample sources of the guide kernels.  RAW: n x 64 FP32 features (plus
+// directions and weights for training).  GEOM: 4 float4 per sample --
+// (p.xyz, N.x) (N.y, N.z, v.x, v.y) (v.z, w.xyz) (weight, emitter flag, -, -) --
+// encoded against the scene box.  NEE: the renderer's emitter-search queue
+// (hit point, normal, incoming direction).
+enum { SRC_RAW = 0, SRC_GEOM = 1, SRC_NEE = 2 };
+
+struct GuideSrc {
+  const float* raw;
+  const float* dirs;
+  const float* weights;
+  const float4* geom;
+  const float4* nee_a;
+  const float4* nee_b;
+  const float4* nee_c;
+  const float4* ps_att;   // SRC_NEE: path state (emitter flag in .w)
+  const uint32_t* count;  // device sample count, clamped to n; null: use n
+  uint32_t n;             // samples [first, min(count, n)) are used
+  uint32_t first;
+  float bmin[3], bmax[3];
+};
+
+Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s);
+// Fills n training samples from the wave's guided-vertex records (host
+// launcher in wavefront.cu).
+Status guide_collect(Renderer& r, int wave, int scene, cudaStream_t s);
+// outputs: max_n x 40 floats (entries beyond the live count are not written)
+Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n,
+                          cudaStream_t s);
+// zeroes the gradient and loss, then accumulates them over the samples
+Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
+                          cudaStream_t s);
+Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s);
+Status guide_check_status(GuideNet& g, cudaStream_t s);
 Status guide_renderer_init(Renderer& r);
 
 }  // namespace lisa
+
+// C-ABI handle of a guide: owns its network, or borrows a renderer's.
+struct lisa_guide {
+  std::unique_ptr<lisa::GuideNet> net;  // owned network
+  lisa::GuideNet* borrowed = nullptr;   // a renderer's network
+  cudaStream_t stream = nullptr;
+  bool owns_stream = true;
+  lisa::GuideNet& get() { return borrowed ? *borrowed : *net; }
+};

@@ -19,20 +19,23 @@ namespace guide {
 constexpr int LOBES = 8;
 constexpr int NOUT = 40;
 constexpr int NIN = 64;
-constexpr float KAPPA_LO = -4.0f, KAPPA_HI = 5.0f;  // kappa = exp(raw), raw clamped
+constexpr float KAPPA_LO = -4.0f, KAPPA_HI = 8.0f;  // kappa = exp(raw), raw clamped
 
 // Input features (64): sin(2^k pi x) of the position normalised to the
-// scene box, k = 0..11, for x, y, z (36); the normalised position mapped to
-// [-1, 1] (3); the shading normal (3); the view direction (3); their dot
-// product (1); zeros (18).
+// scene box, twelve octaves k = -3..8, for x, y, z (36); the normalised
+// position mapped to [-1, 1] (3); the shading normal (3); the view
+// direction (3); their dot product (1); the estimator's emitter flag after
+// this vertex's emitter search (1: an emitter was seen and the flag is
+// set, shader.cu:177-184), which changes what a bounce will gather; zeros
+// (17).
 __device__ __forceinline__ void encode(const float* bmin, const float* bmax, float px, float py, float pz, float nx,
-                                       float ny, float nz, float vx, float vy, float vz, float* f) {
+                                       float ny, float nz, float vx, float vy, float vz, float flag, float* f) {
   const float p[3] = {px, py, pz};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float ext = bmax[a] - bmin[a];
     const float u = ext > 0.0f ? fminf(fmaxf((p[a] - bmin[a]) / ext, 0.0f), 1.0f) : 0.5f;
-    float s = u;
+    float s = u * 0.125f;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
       f[3 * k + a] = sinpif(s);
@@ -47,8 +50,9 @@ __device__ __forceinline__ void encode(const float* bmin, const float* bmax, flo
   f[43] = vy;
   f[44] = vz;
   f[45] = nx * vx + ny * vy + nz * vz;
+  f[46] = flag;
 #pragma unroll
-  for (int i = 46; i < 64; ++i) f[i] = 0.0f;
+  for (int i = 47; i < 64; ++i) f[i] = 0.0f;
 }
 
 struct Lobe {

@@ -106,7 +106,8 @@ struct WaveCtrl {
   uint32_t train_count;
   uint32_t head[4];
   uint32_t status;
-  uint32_t pad[3];
+  uint32_t guided_count;  // guided vertices of the current wave
+  uint32_t pad[2];
   unsigned long long rays_primary;
   unsigned long long rays_bounce;
   unsigned long long rays_shadow;

@@ -127,6 +127,8 @@ struct SceneGpu {
   uint32_t num_prims = 0;
   uint32_t npix = 0;
   uint64_t samples_done = 0;  // samples per pixel accumulated
+  uint64_t sample_offset = 0; // first sample index of this renderer's range
+  uint64_t next_sample = 0;   // index of the next sample to render
   uint32_t subframe = 0;      // progressive launches done
   BvhBuildResult bvh;
   // device
@@ -181,10 +183,16 @@ struct Renderer {
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<uint64_t> graph_key;
   std::vector<std::pair<int, std::pair<size_t, size_t>>> graph_marks;
-  uint32_t graph_launches[4] = {0, 0, 0, 0};
+  uint32_t graph_launches[5] = {0, 0, 0, 0, 0};  // trace, shade, nee, total, guide
   // guided mode
   std::vector<std::unique_ptr<GuideNet>> guides;
-  void* guide_bufs = nullptr;
+  float* guide_out = nullptr;    // capacity x 40 network outputs
+  float4* train_rec = nullptr;   // capacity x max_depth x 5 training records
+  float4* guide_batch = nullptr; // guide_batch_cap x 4 training samples
+  uint32_t guide_batch_cap = 0;  // samples collected per wave
+  uint32_t guide_chunk = 0;      // samples per Adam step
+  uint32_t max_depth = 0;
+  uint64_t guide_waves_done = 0; // waves rendered in guided mode so far
   ~Renderer();
 };
 

@@ -20,6 +20,8 @@
 #include <cstring>
 #include <vector>
 
+#include "guide.cuh"
+#include "guide_mix.cuh"
 #include "lisa_device.cuh"
 #include "lisa_internal.h"
 #include "wavefront.cuh"
@@ -62,6 +64,11 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, bool want) {
 __device__ __forceinline__ void warp_add64(unsigned long long* c, uint32_t v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(c, (unsigned long long)v);
+}
+
+__device__ __forceinline__ void warp_add32(uint32_t* c, uint32_t v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(c, v);
 }
 
 __device__ __forceinline__ V3 barycentric_normal(V3 p, const float4* pr) {
@@ -108,6 +115,8 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
     b.ctrl->head[HEAD_TRACE] = 0;
     b.ctrl->head[HEAD_SHADE] = 0;
     b.ctrl->head[HEAD_NEE] = 0;
+    b.ctrl->guided_count = 0;
+    b.ctrl->train_count = 0;
     b.ctrl->rays_primary += w.paths;
   }
   for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < w.paths; slot += gridDim.x * blockDim.x) {
@@ -151,6 +160,9 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
     b.ps_att[slot] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(-1));
     b.ps_col[slot] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float((g.scene << 24) | pix));
     b.ps_rng[slot] = seed;
+    if (b.train_rec)  // guided mode: no training record yet at any depth
+      for (uint32_t d = 0; d < b.max_depth; ++d)
+        b.train_rec[5ull * ((uint64_t)slot * b.max_depth + d) + 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
@@ -311,7 +323,31 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
 // independently, so a warp stays full while its vertices need between 1 and
 // 30 rays of different lengths.
 
-template <bool COUNT>
+// Guided bounce at an opaque vertex with roughness 1, where the reference
+// draws hemi(N) (lambertian.cu:7-13): one-sample MIS between that sampler
+// (probability c) and the guide's vMF mixture.  The path continues with
+// weight p_hemi(w) / (c p_hemi(w) + (1-c) q_guide(w)), so the estimator's
+// expectation is unchanged; directions below the surface get weight 0.
+__device__ __forceinline__ V3 guided_bounce(const float* __restrict__ o, V3 N, uint32_t& seed, float c, float& weight) {
+  guide::Lobe L[guide::LOBES];
+  float raw[guide::NOUT];
+#pragma unroll
+  for (int k = 0; k < guide::NOUT; ++k) raw[k] = __ldg(o + k);
+  guide::decode(raw, L);
+  V3 w;
+  if (rnd(seed) < c) {
+    w = bsdf::shoot_ray_hemisphere(N, seed);
+  } else {
+    const float u0 = rnd(seed), u1 = rnd(seed), u2 = rnd(seed);
+    guide::mix_sample(L, u0, u1, u2, w.x, w.y, w.z);
+  }
+  const float ph = guide::hemi_pdf(N.x, N.y, N.z, w.x, w.y, w.z);
+  const float q = c * ph + (1.0f - c) * guide::mix_pdf(L, w.x, w.y, w.z);
+  weight = (ph > 0.0f && q > 0.0f && isfinite(q)) ? ph / q : 0.0f;
+  return w;
+}
+
+template <bool COUNT, bool GUIDED = false>
 __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->nee_count;
@@ -358,11 +394,17 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
             const V3 col = ld3(c) + (v3(em.emission[0], em.emission[1], em.emission[2]) * brdf) * att;
             b.ps_col[slot] = make_float4(col.x, col.y, col.z, c.w);
           }
-          // the bounce is drawn at every vertex, the last one included, so
-          // the per-pixel stream advances exactly as in the reference
-          const V3 D = ld3(b.nee_c[entry]);
-          nd = bsdf::bounce(D, N, seed, sc->mats[mat_idx]);
-          want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
+          if (GUIDED && sc->mats[mat_idx].roughness == 1.0f) {
+            // the bounce of a guided vertex is drawn by k_guided_bounce,
+            // after the guide has seen the emitter flag this search left
+            want_ray = false;
+          } else {
+            const V3 D = ld3(b.nee_c[entry]);
+            // the bounce is drawn at every vertex, the last one included, so
+            // the per-pixel stream advances exactly as in the reference
+            nd = bsdf::bounce(D, N, seed, sc->mats[mat_idx]);
+            want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
+          }
           b.ps_rng[slot] = seed;
           b.ps_att[slot] = make_float4(att.x, att.y, att.z, __int_as_float(stale));
           have = false;
@@ -426,6 +468,62 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
 }
 
 // ---------------------------------------------------------------------------
+// guided bounce of the opaque vertices with roughness 1 (deferred by k_nee
+// until the guide's inference has run on the post-search state), with a
+// training record per vertex: the radiance later gathered along the new
+// direction, over the throughput after the bounce, is the incident radiance.
+
+__global__ void __launch_bounds__(256) k_guided_bounce(WaveBufs b, int depth) {
+  const int q = depth & 1;
+  const uint32_t count = *(volatile uint32_t*)&b.ctrl->nee_count;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  uint32_t guided_n = 0;
+  for (uint32_t base = gw * 32; base < count; base += warps * 32) {
+    const uint32_t i = base + lane;
+    bool want = false;
+    V3 p = v3(0.0f), nd = v3(0.0f);
+    uint32_t slot = 0;
+    if (i < count) {
+      const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
+      slot = __float_as_uint(a4.w);
+      const float4 cw = b.ps_col[slot];
+      const SceneDev& sc = b.scenes[__float_as_uint(cw.w) >> 24];
+      const int mat = __float_as_int(b4.w);
+      if (sc.mats[mat].roughness == 1.0f) {
+        p = ld3(a4);
+        const V3 N = ld3(b4);
+        const V3 D = ld3(b.nee_c[i]);
+        uint32_t seed = b.ps_rng[slot];
+        const float4 at = b.ps_att[slot];
+        const int stale = __float_as_int(at.w);
+        float weight;
+        nd = guided_bounce(b.guide_out + 40ull * i, N, seed, b.bsdf_fraction, weight);
+        const V3 att = ld3(at) * weight;
+        want = depth + 1 < (int)sc.num_bounces && weight > 0.0f;
+        const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
+        float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + depth);
+        rec[0] = make_float4(p.x, p.y, p.z, weight);
+        rec[1] = make_float4(N.x, N.y, N.z, nd.x);
+        rec[2] = make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y);
+        rec[3] = make_float4(att.x, att.y, att.z, nd.z);
+        rec[4] = make_float4(cw.x, cw.y, cw.z, stale >= 0 ? 2.0f : 1.0f);  // 0 = no record
+        b.ps_rng[slot] = seed;
+        b.ps_att[slot] = make_float4(att.x, att.y, att.z, at.w);
+        ++guided_n;
+      }
+    }
+    const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want);
+    if (want) {
+      b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
+      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+    }
+  }
+  warp_add32(&b.ctrl->guided_count, guided_n);
+}
+
+// ---------------------------------------------------------------------------
 // accumulate: per pixel, the wave's samples in sample order
 
 __global__ void k_accumulate(WaveBufs b, const WaveDesc* __restrict__ wave) {
@@ -473,6 +571,61 @@ __global__ void k_accumulate(WaveBufs b, const WaveDesc* __restrict__ wave) {
       sc.acc_sum64[3ull * pix + 2] = m2;
     }
     if (w.rng_mode == LISA_RNG_PER_PIXEL) sc.pix_rng[pix] = b.ps_rng[last_slot];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// guide training samples from the wave's guided vertices
+//
+// Each record holds the radiance the path had gathered when the vertex was
+// left (c0) and the throughput after its bounce (a1); with the path's final
+// radiance c, the radiance that arrived along the sampled direction is
+// L = (c - c0) / a1.  The training weight is mean(L) * p_bsdf / q, the
+// importance weight of the Neural Importance Sampling loss.  About `cap`
+// samples are kept, uniformly at random over the wave.
+
+__global__ void k_guide_collect(WaveBufs b, const WaveDesc* __restrict__ wave, float4* __restrict__ batch,
+                                uint32_t cap, uint32_t salt) {
+  const WaveDesc& w = *wave;
+  const uint32_t total = *(volatile uint32_t*)&b.ctrl->guided_count;
+  const float keep = total > cap ? (float)cap / (float)total : 1.0f;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t end = (w.paths + 31u) & ~31u;
+  for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < end; slot += stride) {
+    const bool live = slot < w.paths;
+    const float4 col = live ? b.ps_col[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (uint32_t d = 0; d < b.max_depth; ++d) {
+      bool want = false;
+      float4 r0, r1, r2, r3;
+      float wt = 0.0f, flag = 0.0f;
+      if (live) {
+        const float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + d);
+        const float4 r4 = rec[4];
+        if (r4.w != 0.0f) {
+          flag = r4.w - 1.0f;
+          r0 = rec[0];
+          r1 = rec[1];
+          r2 = rec[2];
+          r3 = rec[3];
+          float l = 0.0f;
+          int nl = 0;
+          if (r3.x > 0.0f) { l += (col.x - r4.x) / r3.x; ++nl; }
+          if (r3.y > 0.0f) { l += (col.y - r4.y) / r3.y; ++nl; }
+          if (r3.z > 0.0f) { l += (col.z - r4.z) / r3.z; ++nl; }
+          wt = nl ? l / (float)nl * r0.w : 0.0f;
+          const float u = (float)(tea<4>(slot * 16u + d, salt) >> 8) * (1.0f / 16777216.0f);
+          want = wt > 0.0f && isfinite(wt) && u < keep;
+        }
+      }
+      const uint32_t i = warp_reserve(&b.ctrl->train_count, want);
+      if (want && i < cap) {
+        float4* o = batch + 4ull * i;
+        o[0] = make_float4(r0.x, r0.y, r0.z, r1.x);
+        o[1] = make_float4(r1.y, r1.z, r2.x, r2.y);
+        o[2] = make_float4(r2.z, r1.w, r2.w, r3.w);
+        o[3] = make_float4(fminf(wt, 1e4f), flag, 0.0f, 0.0f);
+      }
+    }
   }
 }
 
@@ -558,14 +711,24 @@ __global__ void k_brute_rays(const SceneDev* __restrict__ scd, const float* __re
 // ---------------------------------------------------------------------------
 // host side
 
+// Host view of one planned wave.
+struct WaveLaunch {
+  uint32_t bounces;  // depth of its deepest scene
+  int scene;         // scene of its first group (the only one in guided mode)
+  bool train;        // guided mode: train the guide after this wave
+  bool warm;         // guided mode: warm-up wave, sample the BSDF only
+};
+
 namespace {
 
 void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector<uint64_t>& sample_base,
-                std::vector<WaveDesc>& waves, std::vector<uint32_t>& wave_bounces) {
+                std::vector<WaveDesc>& waves, std::vector<WaveLaunch>& wave_launch) {
   const uint32_t W = r.capacity;
   const bool per_pixel = r.opts.rng == LISA_RNG_PER_PIXEL;
+  // a guided wave serves one scene, so one network runs its inference
+  const bool one_scene = r.opts.mode == LISA_MODE_GUIDED;
   waves.clear();
-  wave_bounces.clear();
+  wave_launch.clear();
   WaveDesc cur;
   std::memset(&cur, 0, sizeof(cur));
   uint32_t cur_b = 0;
@@ -574,7 +737,7 @@ void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector
     cur.rng_mode = r.opts.rng;
     cur.seed = r.opts.seed;
     waves.push_back(cur);
-    wave_bounces.push_back(cur_b);
+    wave_launch.push_back(WaveLaunch{cur_b, (int)cur.groups[0].scene, false, false});
     std::memset(&cur, 0, sizeof(cur));
     cur_b = 0;
   };
@@ -596,6 +759,7 @@ void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector
     uint32_t planes = spp[s];
     uint32_t j = (uint32_t)sample_base[s];
     if (npix == 0 || r.scenes[s].params.num_bounces == 0) continue;
+    if (one_scene) close();
     bool scene_in_cur = false;
     while (planes > 0) {
       const uint32_t room = W - cur.paths;
@@ -645,6 +809,10 @@ WaveBufs make_bufs(Renderer& r) {
   b.ctrl = r.ctrl;
   b.scenes = r.d_scenes;
   b.capacity = r.capacity;
+  b.guide_out = r.guide_out;
+  b.train_rec = r.train_rec;
+  b.max_depth = r.max_depth;
+  b.bsdf_fraction = r.opts.guide_bsdf_fraction;
   return b;
 }
 
@@ -672,46 +840,119 @@ struct StageTimer {
 
 }  // namespace
 
-Status launch_wave_sequence(Renderer& r, const std::vector<uint32_t>& wave_bounces, lisa_render_stats* st,
+Status guide_collect(Renderer& r, int wave, int, cudaStream_t s) {
+  WaveBufs b = make_bufs(r);
+  k_guide_collect<<<r.sm_count * 8, 256, 0, s>>>(b, r.d_waves + wave, r.guide_batch, r.guide_batch_cap,
+                                                 (uint32_t)(r.guide_waves_done + (uint64_t)wave) * 2654435761u + 17u);
+  LISA_CUDA(cudaGetLastError());
+  return Status();
+}
+
+// Stage indices of the timer: 0 trace, 1 shade, 2 emitter search, 3 other,
+// 4 guide (inference, sample collection, training, Adam).
+Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, lisa_render_stats* st,
                             StageTimer* tm) {
   WaveBufs b = make_bufs(r);
-  uint32_t launches[4] = {0, 0, 0, 0};  // trace, shade, nee, total
+  uint32_t launches[5] = {0, 0, 0, 0, 0};  // trace, shade, nee, guide, total
   auto stage = [&](int which, auto&& fn) -> Status {
     size_t e0 = 0, e1 = 0;
     if (tm && tm->on) LISA_TRY(tm->ev(&e0));
-    fn();
+    LISA_TRY(fn());
     LISA_CUDA(cudaGetLastError());
     if (tm && tm->on) {
       LISA_TRY(tm->ev(&e1));
       tm->marks.push_back({which, {e0, e1}});
     }
     if (which < 3) launches[which]++;
-    launches[3]++;
+    if (which == 4) launches[3]++;
+    launches[4]++;
     return Status();
   };
   const int acc_blocks = r.sm_count * 8;
   const bool counting = r.opts.count_traversal != 0;
-  for (size_t wv = 0; wv < wave_bounces.size(); ++wv) {
+  const bool guided = r.opts.mode == LISA_MODE_GUIDED;
+  for (size_t wv = 0; wv < waves.size(); ++wv) {
     const WaveDesc* wd = r.d_waves + wv;
-    LISA_TRY(stage(3, [&] { k_raygen<<<r.sm_count * 8, 256, 0, r.stream>>>(b, wd); }));
-    for (uint32_t d = 0; d < wave_bounces[wv]; ++d) {
+    GuideSrc infer_src, train_src;
+    GuideNet* net = nullptr;
+    if (guided) {
+      const SceneGpu& sg = r.scenes[waves[wv].scene];
+      net = r.guides[sg.guide].get();
+      std::memset(&infer_src, 0, sizeof(infer_src));
+      infer_src.nee_a = r.nee_a;
+      infer_src.nee_b = r.nee_b;
+      infer_src.nee_c = r.nee_c;
+      infer_src.ps_att = r.ps_att;
+      infer_src.count = &r.ctrl->nee_count;
+      infer_src.n = r.capacity;
+      for (int k = 0; k < 3; ++k) {
+        infer_src.bmin[k] = sg.bvh.bmin[k];
+        infer_src.bmax[k] = sg.bvh.bmax[k];
+      }
+      train_src = infer_src;
+      train_src.nee_a = train_src.nee_b = train_src.nee_c = nullptr;
+      train_src.geom = r.guide_batch;
+      train_src.count = &r.ctrl->train_count;
+      train_src.n = r.guide_batch_cap;
+    }
+    LISA_TRY(stage(3, [&] {
+      k_raygen<<<r.sm_count * 8, 256, 0, r.stream>>>(b, wd);
+      return Status();
+    }));
+    for (uint32_t d = 0; d < waves[wv].bounces; ++d) {
       LISA_TRY(stage(0, [&] {
         if (counting) k_trace<true><<<r.trace_blocks, r.trace_threads, 0, r.stream>>>(b, (int)d);
         else k_trace<false><<<r.trace_blocks, r.trace_threads, 0, r.stream>>>(b, (int)d);
+        return Status();
       }));
-      LISA_TRY(stage(1, [&] { k_shade<<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d); }));
+      LISA_TRY(stage(1, [&] {
+        k_shade<<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d);
+        return Status();
+      }));
       LISA_TRY(stage(2, [&] {
-        if (counting) k_nee<true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
-        else k_nee<false><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+        if (guided) {
+          if (counting) k_nee<true, true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+          else k_nee<false, true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+        } else {
+          if (counting) k_nee<true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+          else k_nee<false><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+        }
+        return Status();
       }));
+      if (guided) {
+        LISA_TRY(stage(4, [&] { return guide_launch_infer(*net, infer_src, SRC_NEE, r.guide_out, r.capacity, r.stream); }));
+        LISA_TRY(stage(4, [&] {
+          WaveBufs bw = b;  // warm-up waves sample the BSDF only (c = 1)
+          if (waves[wv].warm) bw.bsdf_fraction = 1.0f;
+          k_guided_bounce<<<r.shade_blocks, 256, 0, r.stream>>>(bw, (int)d);
+          return Status();
+        }));
+      }
     }
-    LISA_TRY(stage(3, [&] { k_accumulate<<<acc_blocks, 256, 0, r.stream>>>(b, wd); }));
+    LISA_TRY(stage(3, [&] {
+      k_accumulate<<<acc_blocks, 256, 0, r.stream>>>(b, wd);
+      return Status();
+    }));
+    if (guided && waves[wv].train) {
+      LISA_TRY(stage(4, [&] { return guide_collect(r, (int)wv, waves[wv].scene, r.stream); }));
+      // one Adam step per slice of the collected samples
+      for (uint32_t k = 0; k * r.guide_chunk < r.guide_batch_cap; ++k) {
+        GuideSrc slice = train_src;
+        slice.first = k * r.guide_chunk;
+        slice.n = (k + 1) * r.guide_chunk;
+        LISA_TRY(stage(4, [&] {
+          return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream);
+        }));
+        LISA_TRY(stage(4, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream); }));
+      }
+    }
   }
   if (st) {
     st->launches_trace += launches[0];
     st->launches_shade += launches[1];
     st->launches_nee += launches[2];
-    st->launches_total += launches[3];
+    st->launches_guide += launches[3];
+    st->launches_total += launches[4];
   }
   return Status();
 }
@@ -723,11 +964,17 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   std::vector<uint64_t> base(r.scenes.size());
   for (size_t s = 0; s < r.scenes.size(); ++s) {
     spp[s] = progressive ? spp_req : r.scenes[s].params.num_samples;
-    base[s] = r.scenes[s].samples_done;
+    base[s] = r.scenes[s].next_sample;
   }
   std::vector<WaveDesc> waves;
-  std::vector<uint32_t> wb;
+  std::vector<WaveLaunch> wb;
   plan_waves(r, spp, base, waves, wb);
+  const bool guided = r.opts.mode == LISA_MODE_GUIDED;
+  if (guided)
+    for (size_t i = 0; i < wb.size(); ++i) {
+      wb[i].train = r.opts.guide_train_waves == 0 || r.guide_waves_done + i < r.opts.guide_train_waves;
+      wb[i].warm = r.guide_waves_done + i < r.opts.guide_warmup_waves;
+    }
   if (waves.size() > r.wave_capacity) {
     if (r.d_waves) cudaFree(r.d_waves);
     r.d_waves = nullptr;
@@ -755,14 +1002,17 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   if (r.opts.use_graph && !wb.empty()) {
     // one graph per launch-sequence shape; the wave table it reads is
     // refreshed above, outside the graph
-    std::vector<uint64_t> key(wb.begin(), wb.end());
+    std::vector<uint64_t> key;
+    for (const WaveLaunch& w : wb)
+      key.push_back(((uint64_t)w.bounces << 32) | ((uint64_t)w.scene << 2) | ((uint64_t)w.warm << 1) | w.train);
     key.push_back(r.opts.count_traversal);
     key.push_back(r.opts.stage_timing);
     key.push_back((uint64_t)(uintptr_t)r.d_waves);
     if (key != r.graph_key || !r.graph_exec) {
       if (tm.on) {  // create the timing events before capture begins
         size_t need = 0;
-        for (uint32_t d : wb) need += 2ull * (3ull * d + 2);
+        const uint64_t steps = std::max<uint32_t>(1, r.opts.guide_steps_per_wave);
+        for (const WaveLaunch& w : wb) need += 2ull * (5ull * w.bounces + 6 + 2 * steps);
         while (r.ev_pool.size() < need) {
           cudaEvent_t e;
           LISA_CUDA(cudaEventCreate(&e));
@@ -793,6 +1043,7 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
         r.graph_launches[1] = counts.launches_shade;
         r.graph_launches[2] = counts.launches_nee;
         r.graph_launches[3] = counts.launches_total;
+        r.graph_launches[4] = counts.launches_guide;
       }
     }
     if (s.ok()) {
@@ -801,6 +1052,7 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
       local.launches_shade = r.graph_launches[1];
       local.launches_nee = r.graph_launches[2];
       local.launches_total = r.graph_launches[3];
+      local.launches_guide = r.graph_launches[4];
       const cudaError_t le = cudaGraphLaunch(r.graph_exec, r.stream);
       if (le != cudaSuccess) s = Status::cuda(le, "cudaGraphLaunch");
     }
@@ -828,12 +1080,23 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
       if (m.first == 0) local.ms_trace += t;
       else if (m.first == 1) local.ms_shade += t;
       else if (m.first == 2) local.ms_nee += t;
+      else if (m.first == 4) local.ms_guide += t;
       else local.ms_other += t;
     }
   }
   for (size_t k = 0; k < r.scenes.size(); ++k) {
     r.scenes[k].samples_done += spp[k];
+    r.scenes[k].next_sample += spp[k];
     if (progressive) r.scenes[k].subframe++;
+  }
+  if (guided) {
+    r.guide_waves_done += wb.size();
+    for (auto& g : r.guides) LISA_TRY(guide_check_status(*g, r.stream));
+    if (!wb.empty()) {
+      float l = 0.0f;
+      LISA_CUDA(cudaMemcpy(&l, r.guides[r.scenes[wb.back().scene].guide]->loss, sizeof(float), cudaMemcpyDeviceToHost));
+      local.guide_loss = l;
+    }
   }
   local.rays_primary = hc.rays_primary;
   local.rays_bounce = hc.rays_bounce;
@@ -859,6 +1122,7 @@ Status renderer_reset(Renderer& r) {
     LISA_CUDA(cudaMemsetAsync(s.acc_sq, 0, sizeof(double) * 3 * s.npix, r.stream));
     if (s.acc_sum64) LISA_CUDA(cudaMemsetAsync(s.acc_sum64, 0, sizeof(double) * 3 * s.npix, r.stream));
     s.samples_done = 0;
+    s.next_sample = s.sample_offset;
     s.subframe = 0;
   }
   LISA_CUDA(cudaStreamSynchronize(r.stream));

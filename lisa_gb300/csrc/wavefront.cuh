@@ -22,9 +22,14 @@ struct WaveBufs {
   uint32_t capacity;
   // guided mode (null otherwise)
   float* guide_out;   // per NEE entry: 40 network outputs -> mixture params
-  float4* train_rec;  // per slot and depth: guide training records
+  float4* train_rec;  // per slot and depth: 5 float4 training record
   uint32_t max_depth;
+  float bsdf_fraction;  // one-sample MIS: probability of the BSDF strategy
 };
+
+// Training record of one guided vertex (5 float4, slot-major, depth-minor):
+//   (p.xyz, weight = p_bsdf/q)  (N.xyz, w.x)  (view.xyz, w.y)
+//   (throughput after the bounce .xyz, w.z)  (radiance so far .xyz, valid)
 
 struct GuideSampling {
   float bsdf_fraction;  // c in q = c p_bsdf + (1-c) p_guide

@@ -19,7 +19,7 @@ P_W5 = 4 * 64 * 64
 P_B = P_W5 + 40 * 64
 P_B5 = P_B + 4 * 64
 NPARAM = P_B5 + 40
-KLO, KHI = -4.0, 5.0
+KLO, KHI = -4.0, 8.0
 
 
 def bf16(x):
