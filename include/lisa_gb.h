@@ -114,7 +114,13 @@ typedef struct lisa_options {
                                 BSDF only                                      */
   uint32_t guide_steps_per_wave;/* Adam steps per wave, each on its own slice
                                 of guide_train_batch samples (0 = 1)           */
-  uint32_t reserved1;
+  uint32_t guide_spp_per_wave;/* guided mode: at most this many samples per
+                                pixel per wave, so every scene trains over
+                                several waves (0 = fill the wavefront)         */
+  uint32_t refill_idle;      /* persistent traversal kernels take new work once
+                                this many of a warp's 32 lanes are idle
+                                (1..32; 0 = 12)                               */
+  uint32_t reserved2;
 } lisa_options;
 
 /* Per-call statistics.  Ray counts are rays actually traced: primary +
@@ -271,6 +277,39 @@ int lisa_trace_count(lisa_renderer* r, const float* rays, uint32_t n, uint64_t* 
 /* BVH statistics: 8-wide node count, leaf triangle slots, depth. */
 int lisa_bvh_info(lisa_renderer* r, int32_t scene, uint32_t* nodes, uint32_t* tri_slots,
                   uint32_t* depth, double* build_ms);
+
+/* ---- autotuner (no reference counterpart; the reference launches one fixed
+ * optixLaunch(w, h, 1), render.cc:46-55) ---------------------------------- */
+
+/* Queue and tile sizes for a workload: the wavefront size (paths in flight,
+ * which sizes every ray/hit/path-state queue), the block size of the
+ * persistent traversal kernels and their refill threshold. */
+typedef struct lisa_tuning {
+  uint32_t struct_size;        /* sizeof(lisa_tuning)                          */
+  uint32_t paths_in_flight;
+  uint32_t threads_per_block;
+  uint32_t blocks_per_sm;      /* 0 = as many as fit                           */
+  uint32_t refill_idle;
+  uint32_t candidates;         /* configurations timed (0 = from the cache)    */
+  uint32_t probe_spp;          /* spp of every scene per timed probe render    */
+  uint32_t reserved;
+  double mrays_per_s;          /* probe throughput of the chosen configuration */
+  char key[160];               /* device + bucketed workload signature         */
+} lisa_tuning;
+
+/* Times short progressive renders of the workload (`n` scenes, options
+ * `base`, NULL = defaults) under candidate queue and block sizes and
+ * returns the fastest.  With a non-NULL `cache_path` (a JSON file) a workload
+ * of the same signature on the same device is answered from the file, and a
+ * new choice is added to it. */
+int lisa_autotune(const lisa_renderer_params* scenes, int32_t n, const lisa_options* base,
+                  const char* cache_path, lisa_tuning* out);
+/* Copies the tuned sizes into options. */
+void lisa_tuning_apply(const lisa_tuning* t, lisa_options* o);
+/* Host-only access to a tuning cache file: look a key up (*found = 0 or 1),
+ * or add / replace the entry `t->key`. */
+int lisa_tuning_cache_lookup(const char* cache_path, const char* key, lisa_tuning* out, int32_t* found);
+int lisa_tuning_cache_store(const char* cache_path, const lisa_tuning* t);
 
 /* ---- path guide (no reference counterpart) ------------------------------ */
 

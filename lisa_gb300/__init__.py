@@ -18,10 +18,11 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _native as N
-from ._native import LisaError, Options, RenderStats, default_options  # noqa: F401
+from ._native import LisaError, Options, RenderStats, Tuning, default_options  # noqa: F401
 
 __all__ = ["SceneParser", "Params", "Renderer", "Guide", "render", "display", "params_from_arrays",
-           "params_from_scene", "write_ppm", "LisaError", "default_options"]
+           "params_from_scene", "write_ppm", "LisaError", "default_options", "autotune", "apply_tuning",
+           "tuning_cache_lookup", "tuning_cache_store", "Tuning"]
 
 
 def _ptr(a: Optional[np.ndarray]):
@@ -312,3 +313,34 @@ def write_ppm(path: str, rgba8: np.ndarray):
     a = np.ascontiguousarray(np.asarray(rgba8, np.uint8))
     h, w = a.shape[:2]
     N.check(N.lib().lisa_write_ppm(path.encode(), _ptr(a), w, h))
+
+
+def autotune(params, options: Optional[Options] = None, cache: Optional[str] = None, **opt_kw) -> N.Tuning:
+    """Queue and block sizes for the workload `params` (one Params or a list),
+    timed on the GPU under `options` (or defaults with `opt_kw`); with
+    `cache`, a JSON file answers repeated workloads.  Returns a Tuning;
+    ``apply_tuning`` copies it into options."""
+    if isinstance(params, Params):
+        params = [params]
+    params = list(params)
+    arr = (N.RendererParams * len(params))(*[p.raw for p in params])
+    o = options if options is not None else default_options(**opt_kw)
+    t = N.Tuning()
+    N.check(N.lib().lisa_autotune(arr, len(params), C.byref(o), cache.encode() if cache else None, C.byref(t)))
+    return t
+
+
+def apply_tuning(tuning: N.Tuning, options: Optional[Options] = None, **opt_kw) -> Options:
+    o = options if options is not None else default_options(**opt_kw)
+    N.lib().lisa_tuning_apply(C.byref(tuning), C.byref(o))
+    return o
+
+
+def tuning_cache_lookup(path: str, key: str) -> Optional[N.Tuning]:
+    t, found = N.Tuning(), C.c_int32(0)
+    N.check(N.lib().lisa_tuning_cache_lookup(path.encode(), key.encode(), C.byref(t), C.byref(found)))
+    return t if found.value else None
+
+
+def tuning_cache_store(path: str, tuning: N.Tuning) -> None:
+    N.check(N.lib().lisa_tuning_cache_store(path.encode(), C.byref(tuning)))

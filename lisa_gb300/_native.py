@@ -65,7 +65,8 @@ class Options(C.Structure):
                 ("guide_train_batch", C.c_uint32), ("guide_train_waves", C.c_uint32),
                 ("alloc_cap_bytes", C.c_uint64), ("count_traversal", C.c_uint32),
                 ("guide_warmup_waves", C.c_uint32), ("guide_steps_per_wave", C.c_uint32),
-                ("reserved1", C.c_uint32)]
+                ("guide_spp_per_wave", C.c_uint32), ("refill_idle", C.c_uint32),
+                ("reserved2", C.c_uint32)]
 
 
 class RenderStats(C.Structure):
@@ -86,6 +87,18 @@ class RenderStats(C.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("paths_in_flight", C.c_uint32),
+                ("threads_per_block", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("refill_idle", C.c_uint32), ("candidates", C.c_uint32), ("probe_spp", C.c_uint32),
+                ("reserved", C.c_uint32), ("mrays_per_s", C.c_double), ("key", C.c_char * 160)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("struct_size", "reserved", "key")}
+        d["key"] = self.key.decode()
+        return d
 
 
 # name -> (restype, argtypes); every symbol include/lisa_gb.h declares
@@ -120,6 +133,10 @@ SIGNATURES = {
     "lisa_trace_soup_noalloc": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _P, _P, _P]),
     "lisa_bvh_info": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                 C.POINTER(C.c_uint32), C.POINTER(C.c_double)]),
+    "lisa_autotune": (C.c_int, [_P, C.c_int32, _P, C.c_char_p, _P]),
+    "lisa_tuning_apply": (None, [_P, _P]),
+    "lisa_tuning_cache_lookup": (C.c_int, [C.c_char_p, C.c_char_p, _P, C.POINTER(C.c_int32)]),
+    "lisa_tuning_cache_store": (C.c_int, [C.c_char_p, _P]),
     "lisa_guide_create": (C.c_int, [C.c_uint32, C.POINTER(_P)]),
     "lisa_guide_destroy": (None, [_P]),
     "lisa_guide_get_params": (C.c_int, [_P, _P]),

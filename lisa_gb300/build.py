@@ -26,7 +26,7 @@ CLI = os.path.join(HERE, "bin", "lisa")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", os.path.join(ROOT, "include"), "-I", CSRC,
           "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
-SOURCES = ["api.cu", "bvh_build.cu", "wavefront.cu", "guide.cu", "noalloc.cu", "scene_parser.cc"]
+SOURCES = ["api.cu", "bvh_build.cu", "wavefront.cu", "guide.cu", "noalloc.cu", "autotune.cu", "scene_parser.cc"]
 
 
 def nvcc() -> str:

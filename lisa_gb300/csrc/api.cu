@@ -464,8 +464,13 @@ void lisa_options_default(lisa_options* o) {
   o->rng = LISA_RNG_PER_SAMPLE;
   o->use_graph = 1;
   o->guide_bsdf_fraction = 0.5f;
-  o->guide_lr = 1e-2f;
-  o->guide_train_batch = 1u << 16;
+  // 16 Adam steps of 8192 samples per wave at lr 3e-3, after 4 warm-up
+  // waves, with at most 16 spp per wave
+  o->guide_lr = 3e-3f;
+  o->guide_train_batch = 8192;
+  o->guide_warmup_waves = 4;
+  o->guide_steps_per_wave = 16;
+  o->guide_spp_per_wave = 16;
 }
 
 int lisa_renderer_create(const lisa_renderer_params* params, const lisa_options* opts, lisa_renderer** out) {

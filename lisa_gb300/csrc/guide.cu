@@ -71,17 +71,33 @@ __global__ void k_guide_pack(const float* __restrict__ master, uint16_t* __restr
   *(uint16_t*)(base + tc::sw128_offset(row & 7, k)) = f2bf(v);
 }
 
-// Adam (Kingma & Ba 2015) on the FP32 master parameters.  The step count
-// lives on the device (incremented by k_guide_step afterwards), so a
-// captured graph replays with the right bias correction.
+
+__device__ __forceinline__ void pack_store(uint16_t* pack, int row, int col, float v) {
+  uint8_t* base = (uint8_t*)pack + (size_t)(row & ~7) * 128;
+  *(uint16_t*)(base + tc::sw128_offset(row & 7, col)) = f2bf(v);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters, fused with what
+// follows a step: the BF16 forward and transposed copies of each updated
+// weight are written in place (the zero padding rows never change), the
+// gradient is cleared for the next step and the summed loss is handed to
+// loss_last.  The step count lives on the device (the training kernel
+// increments it), so a captured graph replays with the right bias
+// correction.
 __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
-                             const float* __restrict__ g, float lr, const uint32_t* __restrict__ step,
-                             uint32_t* status) {
+                             float* __restrict__ g, float* __restrict__ loss, float* __restrict__ loss_last,
+                             float lr, const uint32_t* __restrict__ step, uint32_t* status,
+                             uint16_t* __restrict__ pack) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    *loss_last = *loss;
+    *loss = 0.0f;
+  }
   if (i >= NPARAM) return;
-  const float t = (float)(*step + 1);
+  const float t = (float)max(*step, 1u);
   const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
   const float gi = g[i];
+  g[i] = 0.0f;
   if (!isfinite(gi)) {
     atomicOr(status, ST_GUIDE_NONFINITE);
     return;
@@ -90,10 +106,18 @@ __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, 
   const float vi = 0.999f * v[i] + 0.001f * gi * gi;
   m[i] = mi;
   v[i] = vi;
-  master[i] -= lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
+  const float w = master[i] - lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
+  master[i] = w;
+  if (i < P_W5) {  // W1..W4 (output o, input k): forward row l*64+o; transposed for l >= 1
+    const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
+    pack_store(pack, R_FWD + l * 64 + o, k, w);
+    if (l >= 1) pack_store(pack, R_T + (l - 1) * 64 + k, o, w);
+  } else if (i < P_B) {  // W5: forward row R_W5+o, transposed block 3
+    const int o = (i - P_W5) >> 6, k = (i - P_W5) & 63;
+    pack_store(pack, R_W5 + o, k, w);
+    pack_store(pack, R_T + 3 * 64 + k, o, w);
+  }
 }
-
-__global__ void k_guide_step(uint32_t* step) { *step += 1; }
 
 template <int SRC>
 __device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, float* f) {
@@ -278,7 +302,8 @@ __device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int c
 template <int SRC>
 __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restrict__ pack, const float* __restrict__ master,
                                                         GuideSrc src, float inv_n, float* __restrict__ grads,
-                                                        float* __restrict__ loss_out, uint32_t* status) {
+                                                        float* __restrict__ loss_out, uint32_t* status,
+                                                        uint32_t* __restrict__ step_bump) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
@@ -294,6 +319,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   // samples [src.first, n)
   const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
   const uint32_t ntiles = (n - src.first + 127) / 128;
+  if (step_bump && blockIdx.x == 0 && threadIdx.x == 0) *step_bump += 1;  // the Adam step that follows
   if (blockIdx.x >= ntiles) return;
   if (tid == 0) {
     tc::mbar_init(&mbar, 1);
@@ -476,6 +502,7 @@ GuideNet::~GuideNet() {
   if (grads) cudaFree(grads);
   if (w_bf16) cudaFree(w_bf16);
   if (loss) cudaFree(loss);
+  if (loss_last) cudaFree(loss_last);
   if (status) cudaFree(status);
   if (d_step) cudaFree(d_step);
 }
@@ -489,6 +516,7 @@ Status guide_alloc(GuideNet& g) {
   LISA_CUDA(cudaMalloc(&g.grads, sizeof(float) * NPARAM));
   LISA_CUDA(cudaMalloc(&g.w_bf16, PACK_BYTES));
   LISA_CUDA(cudaMalloc(&g.loss, sizeof(float)));
+  LISA_CUDA(cudaMalloc(&g.loss_last, sizeof(float)));
   LISA_CUDA(cudaMalloc(&g.status, sizeof(uint32_t)));
   LISA_CUDA(cudaMalloc(&g.d_step, sizeof(uint32_t)));
   LISA_CUDA(cudaMemset(g.d_step, 0, sizeof(uint32_t)));
@@ -496,6 +524,7 @@ Status guide_alloc(GuideNet& g) {
   LISA_CUDA(cudaMemset(g.adam_v, 0, sizeof(float) * NPARAM));
   LISA_CUDA(cudaMemset(g.grads, 0, sizeof(float) * NPARAM));
   LISA_CUDA(cudaMemset(g.loss, 0, sizeof(float)));
+  LISA_CUDA(cudaMemset(g.loss_last, 0, sizeof(float)));
   LISA_CUDA(cudaMemset(g.status, 0, sizeof(uint32_t)));
   return Status();
 }
@@ -558,25 +587,34 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
   return Status();
 }
 
+// Gradient of one batch into g.grads and g.loss.  With zero_first the two
+// accumulators are cleared first; otherwise they must be zero already (the
+// previous Adam step leaves them so).  With adam_follows the device step
+// count advances for the Adam step launched next.
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s) {
-  LISA_CUDA(cudaMemsetAsync(g.grads, 0, sizeof(float) * NPARAM, s));
-  LISA_CUDA(cudaMemsetAsync(g.loss, 0, sizeof(float), s));
+                          cudaStream_t s, bool zero_first, bool adam_follows) {
+  if (zero_first) {
+    LISA_CUDA(cudaMemsetAsync(g.grads, 0, sizeof(float) * NPARAM, s));
+    LISA_CUDA(cudaMemsetAsync(g.loss, 0, sizeof(float), s));
+  }
   const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
   const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
+  uint32_t* bump = adam_follows ? g.d_step : nullptr;
   if (src_kind == SRC_RAW)
-    k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status);
+    k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status,
+                                                         bump);
   else
-    k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status);
+    k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status,
+                                                          bump);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
 
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
-  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grads, lr, g.d_step, g.status);
-  k_guide_step<<<1, 1, 0, s>>>(g.d_step);
+  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grads, g.loss, g.loss_last, lr,
+                                                    g.d_step, g.status, g.w_bf16);
   LISA_CUDA(cudaGetLastError());
-  return guide_pack(g, s);
+  return Status();
 }
 
 Status guide_check_status(GuideNet& g, cudaStream_t s) {
@@ -710,7 +748,7 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
     src.dirs = d_d;
     src.weights = d_w;
     src.n = n;
-    LISA_TRY(guide_launch_train(g->get(), src, SRC_RAW, 1.0f / (float)n, n, g->stream));
+    LISA_TRY(guide_launch_train(g->get(), src, SRC_RAW, 1.0f / (float)n, n, g->stream, true, lr > 0.0f));
     if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->get().loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     if (grads)
       LISA_CUDA(cudaMemcpyAsync(grads, g->get().grads, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream));

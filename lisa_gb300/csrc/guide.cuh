@@ -19,7 +19,8 @@ struct GuideNet {
   float* adam_v = nullptr;
   float* grads = nullptr;
   uint16_t* w_bf16 = nullptr;
-  float* loss = nullptr;      // device scalar accumulator
+  float* loss = nullptr;      // device scalar accumulator (cleared by each Adam step)
+  float* loss_last = nullptr; // loss of the batch of the last Adam step
   uint32_t* status = nullptr; // device status word (time-outs, non-finite values)
   uint32_t* d_step = nullptr; // Adam step count (device)
   ~GuideNet();
@@ -54,9 +55,13 @@ Status guide_collect(Renderer& r, int wave, int scene, cudaStream_t s);
 // outputs: max_n x 40 floats (entries beyond the live count are not written)
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n,
                           cudaStream_t s);
-// zeroes the gradient and loss, then accumulates them over the samples
+// accumulates the gradient and loss over the samples (zero_first: clear
+// them first; otherwise the previous Adam step left them zero); with
+// adam_follows the device step count advances for the next Adam step
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s);
+                          cudaStream_t s, bool zero_first, bool adam_follows);
+// Adam step; also refreshes the BF16 weights, clears the gradient and moves
+// the loss to loss_last
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s);
 Status guide_check_status(GuideNet& g, cudaStream_t s);
 Status guide_renderer_init(Renderer& r);

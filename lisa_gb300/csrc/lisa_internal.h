@@ -144,10 +144,7 @@ struct SceneGpu {
   float extent = 0.0f;
   float eye[3], U[3], V[3], W[3];
   int guide = -1;
-};
-
-struct WavePlan {
-  std::vector<std::vector<int>> dummy;
+  uint64_t guide_waves_done = 0;  // guided waves of this scene so far
 };
 
 struct Renderer {

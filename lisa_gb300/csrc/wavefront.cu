@@ -39,7 +39,7 @@ constexpr uint32_t FULL = 0xffffffffu;
 #define LISA_NEE_MIN_BLOCKS 7  // 7 x 128 threads per SM (72 registers)
 #endif
 #ifndef LISA_REFILL_IDLE
-#define LISA_REFILL_IDLE 12  // idle lanes (of 32) that trigger a refill round
+#define LISA_REFILL_IDLE 12  // default: idle lanes (of 32) that trigger a refill round
 #endif
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
   bool active = false, exhausted = false;
   while (true) {
     // take new rays only once enough lanes are idle (see k_nee)
-    if (__popc(__ballot_sync(FULL, active)) <= 32 - LISA_REFILL_IDLE) {
+    if (__popc(__ballot_sync(FULL, active)) <= (int)b.refill_busy_max) {
       const bool need = !active && !exhausted;
       const uint32_t nmask = __ballot_sync(FULL, need);
       if (nmask) {
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
     // rays) runs only once enough lanes are idle, so its divergent code is
     // shared by many lanes; otherwise the warp keeps traversing.
     const uint32_t busy = __ballot_sync(FULL, ray_active);
-    if (__popc(busy) <= 32 - LISA_REFILL_IDLE) {
+    if (__popc(busy) <= (int)b.refill_busy_max) {
       bool want_ray = false;
       V3 nd = v3(0.0f);
       if (pending) {
@@ -725,8 +725,10 @@ void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector
                 std::vector<WaveDesc>& waves, std::vector<WaveLaunch>& wave_launch) {
   const uint32_t W = r.capacity;
   const bool per_pixel = r.opts.rng == LISA_RNG_PER_PIXEL;
-  // a guided wave serves one scene, so one network runs its inference
+  // a guided wave serves one scene, so one network runs its inference, and
+  // holds at most guide_spp_per_wave planes so the guide trains in between
   const bool one_scene = r.opts.mode == LISA_MODE_GUIDED;
+  const uint32_t max_planes = one_scene && r.opts.guide_spp_per_wave ? r.opts.guide_spp_per_wave : UINT32_MAX;
   waves.clear();
   wave_launch.clear();
   WaveDesc cur;
@@ -769,12 +771,16 @@ void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector
         continue;
       }
       if (npix <= room) {
-        uint32_t k = std::min(planes, room / npix);
+        uint32_t k = std::min(std::min(planes, room / npix), max_planes);
         if (per_pixel) k = 1;
         add(s, 0, npix, j, k);
         scene_in_cur = true;
         planes -= k;
         j += k;
+        if (one_scene) {
+          close();
+          scene_in_cur = false;
+        }
       } else if (cur.paths == 0) {
         for (uint32_t p0 = 0; p0 < npix; p0 += W) {
           add(s, p0, std::min(W, npix - p0), j, 1);
@@ -809,6 +815,7 @@ WaveBufs make_bufs(Renderer& r) {
   b.ctrl = r.ctrl;
   b.scenes = r.d_scenes;
   b.capacity = r.capacity;
+  b.refill_busy_max = 32u - (r.opts.refill_idle ? std::min<uint32_t>(r.opts.refill_idle, 32u) : LISA_REFILL_IDLE);
   b.guide_out = r.guide_out;
   b.train_rec = r.train_rec;
   b.max_depth = r.max_depth;
@@ -941,7 +948,8 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         slice.first = k * r.guide_chunk;
         slice.n = (k + 1) * r.guide_chunk;
         LISA_TRY(stage(4, [&] {
-          return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream);
+          return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream,
+                                    false, true);
         }));
         LISA_TRY(stage(4, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream); }));
       }
@@ -970,10 +978,13 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   std::vector<WaveLaunch> wb;
   plan_waves(r, spp, base, waves, wb);
   const bool guided = r.opts.mode == LISA_MODE_GUIDED;
+  // warm-up and training flags count the waves of each scene (its guide)
+  std::vector<uint64_t> scene_waves(r.scenes.size(), 0);
   if (guided)
     for (size_t i = 0; i < wb.size(); ++i) {
-      wb[i].train = r.opts.guide_train_waves == 0 || r.guide_waves_done + i < r.opts.guide_train_waves;
-      wb[i].warm = r.guide_waves_done + i < r.opts.guide_warmup_waves;
+      const uint64_t k = r.scenes[wb[i].scene].guide_waves_done + scene_waves[wb[i].scene]++;
+      wb[i].train = r.opts.guide_train_waves == 0 || k < r.opts.guide_train_waves;
+      wb[i].warm = k < r.opts.guide_warmup_waves;
     }
   if (waves.size() > r.wave_capacity) {
     if (r.d_waves) cudaFree(r.d_waves);
@@ -1091,10 +1102,12 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   }
   if (guided) {
     r.guide_waves_done += wb.size();
+    for (size_t k = 0; k < r.scenes.size(); ++k) r.scenes[k].guide_waves_done += scene_waves[k];
     for (auto& g : r.guides) LISA_TRY(guide_check_status(*g, r.stream));
     if (!wb.empty()) {
       float l = 0.0f;
-      LISA_CUDA(cudaMemcpy(&l, r.guides[r.scenes[wb.back().scene].guide]->loss, sizeof(float), cudaMemcpyDeviceToHost));
+      LISA_CUDA(cudaMemcpy(&l, r.guides[r.scenes[wb.back().scene].guide]->loss_last, sizeof(float),
+                           cudaMemcpyDeviceToHost));
       local.guide_loss = l;
     }
   }

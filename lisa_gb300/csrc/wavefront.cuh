@@ -20,6 +20,7 @@ struct WaveBufs {
   WaveCtrl* ctrl;
   const SceneDev* scenes;
   uint32_t capacity;
+  uint32_t refill_busy_max;  // persistent kernels refill a warp once at most this many lanes are busy
   // guided mode (null otherwise)
   float* guide_out;   // per NEE entry: 40 network outputs -> mixture params
   float4* train_rec;  // per slot and depth: 5 float4 training record

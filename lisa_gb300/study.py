@@ -1,0 +1,202 @@
+"""Image-quality studies: guided vs plain sampling at equal time, against a
+high-spp reference accumulated in FP64 on the GPU.
+
+  python -m lisa_gb300.study hard_indirect [--res 1024] [--spp 256] [--ref-spp 16384]
+  python -m lisa_gb300.study batch [--n 64] [--spp-scale 0.0625] [--ref-mult 16]
+
+relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2).
+Because the reference has finite spp, E[(x - ref)^2] = MSE(x) + Var(ref);
+the "corrected" figure subtracts the reference's own per-pixel variance of
+the mean (its FP64 sample variance / its spp), which leaves an unbiased
+estimate of the render's relMSE.  Equal time: Monte Carlo error falls as
+1/spp, so a render that took t_g for relMSE e_g reaches e_g * t_g / t_p in the
+plain render's time t_p; "time to plain's error" is (t_g / t_p) * (e_g / e_p).
+
+Each run prints one JSON line per measurement and, with --summary, writes a
+short markdown table.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+from typing import List
+
+import numpy as np
+
+from . import scenes as S
+
+
+def relmse(x: np.ndarray, ref: np.ndarray, ref_var_of_mean: np.ndarray = None) -> float:
+    d2 = (np.asarray(x, np.float64) - ref) ** 2
+    if ref_var_of_mean is not None:
+        d2 = d2 - ref_var_of_mean
+    return float(np.mean(d2 / (ref * ref + 1e-2)))
+
+
+def _render(L, params, **opt):
+    r = L.Renderer(params, L.default_options(stage_timing=1, **opt))
+    t0 = time.perf_counter()
+    st = r.render()
+    wall = time.perf_counter() - t0
+    return r, st, wall
+
+
+def hard_indirect(args) -> List[dict]:
+    import lisa_gb300 as L
+
+    sc = S.hard_indirect(level=args.level, width=args.res, height=args.res, num_samples=args.spp,
+                         num_bounces=8)
+    out = []
+    # reference: plain sampling, FP64 accumulation, progressive launches
+    p_ref = L.params_from_scene(sc, num_samples=args.ref_spp)
+    ref = L.Renderer(p_ref, L.default_options(accum_fp64=1, seed=1000003))
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.ref_spp:
+        k = min(args.ref_chunk, args.ref_spp - done)
+        ref.render_progressive(k)
+        done += k
+    ref_s = time.perf_counter() - t0
+    _, var, R = ref.image(variance=True, fp64=True)
+    vom = var / args.ref_spp
+    ref.close()
+    p = L.params_from_scene(sc)
+    rows = {}
+    for name, opt in (("plain", dict(seed=12)), ("guided", dict(seed=13, mode=L._native.LISA_MODE_GUIDED))):
+        r, st, wall = _render(L, p, **opt)
+        img = r.image()
+        rows[name] = dict(ms=st.ms_device, wall_s=wall, rays=st.rays, relmse=relmse(img, R),
+                          relmse_corrected=relmse(img, R, vom), guide_loss=st.guide_loss,
+                          stages_ms={"trace": st.ms_trace, "shade": st.ms_shade, "nee": st.ms_nee,
+                                     "guide": st.ms_guide, "other": st.ms_other},
+                          launches=st.launches_total)
+        r.close()
+    tp, tg = rows["plain"]["ms"], rows["guided"]["ms"]
+    ep, eg = rows["plain"]["relmse_corrected"], rows["guided"]["relmse_corrected"]
+    out.append({
+        "study": "hard_indirect", "scene": sc.name, "triangles": sc.num_triangles, "res": args.res,
+        "spp": args.spp, "bounces": 8, "reference": {"spp": args.ref_spp, "accum": "fp64", "seconds": ref_s},
+        "plain": rows["plain"], "guided": rows["guided"],
+        "equal_time_relmse": {"plain": ep, "guided": eg * tg / tp},
+        "time_to_plain_error": (tg / tp) * (eg / ep) if ep > 0 else None,
+    })
+    return out
+
+
+def batch(args) -> List[dict]:
+    import lisa_gb300 as L
+
+    G = L._native.LISA_MODE_GUIDED
+    scs = S.batch_scenes(n=args.n, seed=5, max_res=args.max_res)
+    spp = [max(4, int(round(s.num_samples * args.spp_scale))) for s in scs]
+    params = [L.params_from_scene(s, num_samples=k) for s, k in zip(scs, spp)]
+    tune_p = L.autotune(params, cache=args.cache)
+    tune_g = L.autotune(params, cache=args.cache, mode=G)
+    res = {}
+    imgs = {}
+    for name, tune, opt in (("plain", tune_p, dict(seed=12)), ("guided", tune_g, dict(seed=13, mode=G))):
+        o = L.apply_tuning(tune, L.default_options(**opt))
+        r = L.Renderer(params, o)
+        r.render()  # warm-up: graph capture, guide training from scratch below
+        r.close()
+        r = L.Renderer(params, o)
+        t0 = time.perf_counter()
+        st = r.render()
+        wall = time.perf_counter() - t0
+        res[name] = dict(ms=st.ms_device, wall_s=wall, rays=st.rays, mrays_per_s=st.rays / st.ms_device / 1e3,
+                         launches=st.launches_total, tuning=tune.as_dict())
+        imgs[name] = [r.image(k) for k in range(len(params))]
+        r.close()
+    # per-scene reference: ref_mult x the spp, plain, FP64
+    p_ref = [L.params_from_scene(s, num_samples=k * args.ref_mult) for s, k in zip(scs, spp)]
+    t0 = time.perf_counter()
+    ref = L.Renderer(p_ref, L.apply_tuning(tune_p, L.default_options(accum_fp64=1, seed=1000003)))
+    ref.render()
+    ref_s = time.perf_counter() - t0
+    scenes_out = []
+    tp, tg = res["plain"]["ms"], res["guided"]["ms"]
+    for k, s in enumerate(scs):
+        _, var, R = ref.image(k, variance=True, fp64=True)
+        vom = var / (spp[k] * args.ref_mult)
+        ep = relmse(imgs["plain"][k], R, vom)
+        eg = relmse(imgs["guided"][k], R, vom)
+        scenes_out.append({"scene": s.name, "triangles": s.num_triangles, "res": [s.width, s.height],
+                           "spp": spp[k], "bounces": s.num_bounces, "relmse_plain": ep, "relmse_guided": eg,
+                           "equal_time_guided": eg * tg / tp})
+    ref.close()
+    return [{
+        "study": "batch", "scenes": len(scs), "spp_scale": args.spp_scale,
+        "total_paths": int(sum(s.width * s.height * k for s, k in zip(scs, spp))),
+        "reference": {"spp_mult": args.ref_mult, "accum": "fp64", "seconds": ref_s},
+        "plain": res["plain"], "guided": res["guided"], "per_scene": scenes_out,
+        "median_equal_time_ratio": float(np.median([x["equal_time_guided"] / max(x["relmse_plain"], 1e-30)
+                                                    for x in scenes_out])),
+    }]
+
+
+def summary_md(rows: List[dict], cmd: str) -> str:
+    lines = [f"Command: `{cmd}`", ""]
+    for r in rows:
+        if r["study"] == "hard_indirect":
+            lines += [f"## hard indirect ({r['scene']}, {r['triangles']:,} tris, {r['res']}^2, {r['spp']} spp)", "",
+                      f"Reference: {r['reference']['spp']} spp plain, FP64 accumulation "
+                      f"({r['reference']['seconds']:.0f} s).", "",
+                      "| method | device ms | Mrays | relMSE | relMSE (ref. variance removed) |",
+                      "|---|---|---|---|---|"]
+            for m in ("plain", "guided"):
+                x = r[m]
+                lines.append(f"| {m} | {x['ms']:.1f} | {x['rays'] / 1e6:.0f} | {x['relmse']:.6g} | "
+                             f"{x['relmse_corrected']:.6g} |")
+            lines += ["", f"Equal-time relMSE: plain {r['equal_time_relmse']['plain']:.6g}, guided "
+                          f"{r['equal_time_relmse']['guided']:.6g}; guided time to plain's error = "
+                          f"{r['time_to_plain_error']:.3f} x plain's time.", ""]
+        else:
+            lines += [f"## batch of {r['scenes']} scenes (spp x {r['spp_scale']}, {r['total_paths']:,} paths)", "",
+                      "| method | device ms | Mrays/s | launches | tuning |", "|---|---|---|---|---|"]
+            for m in ("plain", "guided"):
+                x = r[m]
+                t = x["tuning"]
+                lines.append(f"| {m} | {x['ms']:.1f} | {x['mrays_per_s']:.0f} | {x['launches']} | "
+                             f"W={t['paths_in_flight']}, {t['threads_per_block']} thr, refill {t['refill_idle']} |")
+            lines += ["", f"Median over scenes of guided equal-time relMSE / plain relMSE: "
+                          f"{r['median_equal_time_ratio']:.3f}", "",
+                      "| scene | tris | res | spp | bounces | relMSE plain | relMSE guided | guided at equal time |",
+                      "|---|---|---|---|---|---|---|---|"]
+            for s in r["per_scene"]:
+                lines.append(f"| {s['scene']} | {s['triangles']:,} | {s['res'][0]}x{s['res'][1]} | {s['spp']} | "
+                             f"{s['bounces']} | {s['relmse_plain']:.4g} | {s['relmse_guided']:.4g} | "
+                             f"{s['equal_time_guided']:.4g} |")
+            lines.append("")
+    return "\n".join(lines) + "\n"
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m lisa_gb300.study")
+    sub = ap.add_subparsers(dest="which", required=True)
+    h = sub.add_parser("hard_indirect")
+    h.add_argument("--res", type=int, default=1024)
+    h.add_argument("--level", type=int, default=8)
+    h.add_argument("--spp", type=int, default=256)
+    h.add_argument("--ref-spp", type=int, default=16384)
+    h.add_argument("--ref-chunk", type=int, default=256)
+    b = sub.add_parser("batch")
+    b.add_argument("--n", type=int, default=64)
+    b.add_argument("--max-res", type=int, default=1024)
+    b.add_argument("--spp-scale", type=float, default=1.0 / 16)
+    b.add_argument("--ref-mult", type=int, default=16)
+    b.add_argument("--cache", default=None, help="autotuner cache (JSON)")
+    for p in (h, b):
+        p.add_argument("--summary", default=None, help="write a markdown summary here")
+    args = ap.parse_args(argv)
+    rows = hard_indirect(args) if args.which == "hard_indirect" else batch(args)
+    for r in rows:
+        print(json.dumps(r), flush=True)
+    if args.summary:
+        with open(args.summary, "w") as f:
+            f.write(summary_md(rows, "python -m lisa_gb300.study " + " ".join(argv or sys.argv[1:])))
+
+
+if __name__ == "__main__":
+    main()
