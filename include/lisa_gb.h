@@ -84,6 +84,15 @@ typedef struct lisa_renderer_params {
 #define LISA_MODE_GUIDED 1 /* same estimator, bounce drawn from MLP guide+BSDF
                               by one-sample MIS                               */
 
+#define LISA_ESTIMATOR_COMPAT 0   /* the reference estimator (default)      */
+#define LISA_ESTIMATOR_PHYSICAL 1 /* opt-in physically based estimator: emitter
+                                     sampling by area x luminance, cosine-
+                                     weighted diffuse sampling, power-heuristic
+                                     MIS, roughness = weight of the diffuse
+                                     lobe against a mirror, Schlick on the
+                                     less dense side; combines with
+                                     LISA_MODE_GUIDED                         */
+
 #define LISA_RNG_PER_SAMPLE 0 /* one LCG stream per (seed, pixel, sample)    */
 #define LISA_RNG_PER_PIXEL 1  /* the reference stream: tea<16>(pixel,
                                  subframe) shared by all samples of a pixel
@@ -120,7 +129,7 @@ typedef struct lisa_options {
   uint32_t refill_idle;      /* persistent traversal kernels take new work once
                                 this many of a warp's 32 lanes are idle
                                 (1..32; 0 = 12)                               */
-  uint32_t reserved2;
+  uint32_t estimator;        /* LISA_ESTIMATOR_*                               */
 } lisa_options;
 
 /* Per-call statistics.  Ray counts are rays actually traced: primary +

@@ -23,6 +23,8 @@ LISA_ERR_UNSUPPORTED = 7
 
 LISA_MODE_COMPAT = 0
 LISA_MODE_GUIDED = 1
+LISA_ESTIMATOR_COMPAT = 0
+LISA_ESTIMATOR_PHYSICAL = 1
 LISA_RNG_PER_SAMPLE = 0
 LISA_RNG_PER_PIXEL = 1
 
@@ -66,7 +68,7 @@ class Options(C.Structure):
                 ("alloc_cap_bytes", C.c_uint64), ("count_traversal", C.c_uint32),
                 ("guide_warmup_waves", C.c_uint32), ("guide_steps_per_wave", C.c_uint32),
                 ("guide_spp_per_wave", C.c_uint32), ("refill_idle", C.c_uint32),
-                ("reserved2", C.c_uint32)]
+                ("estimator", C.c_uint32)]
 
 
 class RenderStats(C.Structure):

@@ -174,6 +174,64 @@ Status validate(const lisa_renderer_params& p) {
 }
 }  // namespace
 
+// Emitters of the physically based estimator, in triangle order: every
+// emissive triangle of positive area and luminance gets a record
+// (v0, area pdf) (e1 = v1 - v0, material) (e2 = v2 - v0) (unit normal) and a
+// CDF entry over area x luminance; each material gets its area pdf
+// luminance / total.  Float steps as written (no contraction), sums in double.
+Status build_emitters(Renderer& r, const lisa_renderer_params& p, SceneGpu& s, std::vector<DevMaterial>& dm) {
+  const int M = p.num_materials;
+  const uint32_t T = (uint32_t)(p.num_vertices / 3);
+  std::vector<float> lum(std::max(M, 1), 0.0f);
+  for (int m = 0; m < M; ++m)
+    if (dm[m].cls == MAT_EMIT)
+      lum[m] = (0.2126f * dm[m].emission[0] + 0.7152f * dm[m].emission[1]) + 0.0722f * dm[m].emission[2];
+  std::vector<float4> rec;
+  std::vector<double> w;
+  for (uint32_t t = 0; t < T; ++t) {
+    const int m = p.mat_indices[t];
+    if (dm[m].cls != MAT_EMIT || !(lum[m] > 0.0f)) continue;
+    const lisa_float3* v = p.vertices + 3ull * t;
+    const float e1x = v[1].x - v[0].x, e1y = v[1].y - v[0].y, e1z = v[1].z - v[0].z;
+    const float e2x = v[2].x - v[0].x, e2y = v[2].y - v[0].y, e2z = v[2].z - v[0].z;
+    const float cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+    const float len = std::sqrt(cx * cx + cy * cy + cz * cz);
+    const float area = 0.5f * len;
+    if (!(area > 0.0f)) continue;
+    const float inv = 1.0f / len;
+    int32_t mb = m;
+    float mf;
+    std::memcpy(&mf, &mb, 4);
+    rec.push_back(make_float4(v[0].x, v[0].y, v[0].z, 0.0f));
+    rec.push_back(make_float4(e1x, e1y, e1z, mf));
+    rec.push_back(make_float4(e2x, e2y, e2z, 0.0f));
+    rec.push_back(make_float4(cx * inv, cy * inv, cz * inv, 0.0f));
+    w.push_back((double)area * (double)lum[m]);
+  }
+  s.num_emit = (uint32_t)w.size();
+  if (!s.num_emit) return Status();
+  double total = 0.0;
+  for (double x : w) total += x;
+  std::vector<float> cdf(s.num_emit);
+  double acc = 0.0;
+  for (uint32_t i = 0; i < s.num_emit; ++i) {
+    acc += w[i];
+    cdf[i] = (float)(acc / total);
+  }
+  cdf[s.num_emit - 1] = 1.0f;
+  for (int m = 0; m < M; ++m) dm[m].light_pdf = (float)((double)lum[m] / total);
+  for (uint32_t i = 0; i < s.num_emit; ++i) {
+    int32_t m;
+    std::memcpy(&m, &rec[4ull * i + 1].w, 4);
+    rec[4ull * i].w = dm[m].light_pdf;
+  }
+  LISA_TRY(r.arena.alloc((void**)&s.emit, sizeof(float4) * rec.size(), "emitters"));
+  LISA_TRY(r.arena.alloc((void**)&s.emit_cdf, sizeof(float) * cdf.size(), "emitter CDF"));
+  LISA_CUDA(cudaMemcpy(s.emit, rec.data(), sizeof(float4) * rec.size(), cudaMemcpyHostToDevice));
+  LISA_CUDA(cudaMemcpy(s.emit_cdf, cdf.data(), sizeof(float) * cdf.size(), cudaMemcpyHostToDevice));
+  return Status();
+}
+
 Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   LISA_TRY(validate(p));
   s.params = p;
@@ -223,6 +281,7 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   // materials
   std::vector<DevMaterial> dm(std::max(p.num_materials, 1));
   for (int i = 0; i < p.num_materials; ++i) dm[i] = to_dev(p.materials[i]);
+  if (r.opts.estimator == LISA_ESTIMATOR_PHYSICAL) LISA_TRY(build_emitters(r, p, s, dm));
   LISA_TRY(r.arena.alloc((void**)&s.mats, sizeof(DevMaterial) * dm.size(), "materials"));
   LISA_CUDA(cudaMemcpyAsync(s.mats, dm.data(), sizeof(DevMaterial) * dm.size(), cudaMemcpyHostToDevice, r.stream));
   // accumulation
@@ -278,6 +337,9 @@ SceneDev scene_dev(const Renderer& r, const SceneGpu& s) {
   d.acc_sum64 = s.acc_sum64;
   d.pix_rng = s.pix_rng;
   d.guide = s.guide;
+  d.emit = s.emit;
+  d.emit_cdf = s.emit_cdf;
+  d.num_emit = s.num_emit;
   return d;
 }
 
@@ -292,6 +354,7 @@ Status renderer_create(const lisa_renderer_params* scenes, int n, const lisa_opt
   }
   if (r->opts.mode > LISA_MODE_GUIDED) return Status::invalid("unknown mode");
   if (r->opts.rng > LISA_RNG_PER_PIXEL) return Status::invalid("unknown rng mode");
+  if (r->opts.estimator > LISA_ESTIMATOR_PHYSICAL) return Status::invalid("unknown estimator");
   r->arena.cap = r->opts.alloc_cap_bytes;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -464,12 +527,12 @@ void lisa_options_default(lisa_options* o) {
   o->rng = LISA_RNG_PER_SAMPLE;
   o->use_graph = 1;
   o->guide_bsdf_fraction = 0.5f;
-  // 16 Adam steps of 8192 samples per wave at lr 3e-3, after 4 warm-up
+  // 32 Adam steps of 16384 samples per wave at lr 1e-3, after 4 warm-up
   // waves, with at most 16 spp per wave
-  o->guide_lr = 3e-3f;
-  o->guide_train_batch = 8192;
+  o->guide_lr = 1e-3f;
+  o->guide_train_batch = 16384;
   o->guide_warmup_waves = 4;
-  o->guide_steps_per_wave = 16;
+  o->guide_steps_per_wave = 32;
   o->guide_spp_per_wave = 16;
 }
 

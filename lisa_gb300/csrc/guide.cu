@@ -22,32 +22,12 @@
 #include <vector>
 
 #include "guide.cuh"
+#include "guide_infer.cuh"
 #include "guide_mix.cuh"
 #include "lisa_device.cuh"
 #include "tcgen05.cuh"
 
 namespace lisa {
-
-// ---- parameter layout (FP32 master) ------------------------------------------
-constexpr int P_W = 0;                    // W1..W4: 4 x 64 x 64, then W5: 40 x 64
-constexpr int P_W5 = 4 * 64 * 64;
-constexpr int P_B = P_W5 + 40 * 64;       // b1..b4: 4 x 64, then b5: 40
-constexpr int P_B5 = P_B + 4 * 64;
-constexpr int NPARAM = P_B5 + 40;
-static_assert(NPARAM == LISA_GUIDE_NUM_PARAMS, "parameter count");
-
-// ---- packed BF16 weights: rows of 128 B, pre-swizzled in 8-row groups ------------
-constexpr int R_FWD = 0;        // W1..W4 forward: 4 x 64 rows (row = output)
-constexpr int R_W5 = 256;       // W5 forward: 48 rows (40 used)
-constexpr int R_T = 304;        // W2^T..W5^T: 4 x 64 rows (row = input, K = output)
-constexpr int R_TOTAL = 560;
-constexpr int PACK_BYTES = R_TOTAL * 128;
-constexpr int FWD_BYTES = R_T * 128;  // what inference needs
-
-__device__ __forceinline__ uint16_t f2bf(float x) {
-  return __bfloat16_as_ushort(__float2bfloat16_rn(x));
-}
-__device__ __forceinline__ float bf2f(uint16_t h) { return __bfloat162float(__ushort_as_bfloat16(h)); }
 
 // master -> packed BF16 (forward and transposed copies)
 __global__ void k_guide_pack(const float* __restrict__ master, uint16_t* __restrict__ pack) {
@@ -119,157 +99,20 @@ __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, 
   }
 }
 
-template <int SRC>
-__device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, float* f) {
-  if (SRC == SRC_RAW) {
-    const float4* r = (const float4*)(s.raw + 64ull * i);
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const float4 x = __ldg(r + c);
-      f[4 * c] = x.x;
-      f[4 * c + 1] = x.y;
-      f[4 * c + 2] = x.z;
-      f[4 * c + 3] = x.w;
-    }
-  } else if (SRC == SRC_GEOM) {
-    const float4 a = s.geom[4ull * i], b = s.geom[4ull * i + 1], c = s.geom[4ull * i + 2], d = s.geom[4ull * i + 3];
-    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, d.y, f);
-  } else {
-    const float4 a = s.nee_a[i], b = s.nee_b[i], c = s.nee_c[i];
-    // view direction: towards where the ray came from
-    const float il = rsqrtf(fmaxf(c.x * c.x + c.y * c.y + c.z * c.z, 1e-30f));
-    const int stale = __float_as_int(s.ps_att[__float_as_uint(a.w)].w);
-    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il,
-                  stale >= 0 ? 1.0f : 0.0f, f);
-  }
-}
-
-// Writes 64 values as BF16 into row `row` of a swizzled tile.
-__device__ __forceinline__ void store_row_bf16(uint8_t* tile, int row, const float* v) {
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    uint4 q;
-    q.x = (uint32_t)f2bf(v[8 * c + 0]) | ((uint32_t)f2bf(v[8 * c + 1]) << 16);
-    q.y = (uint32_t)f2bf(v[8 * c + 2]) | ((uint32_t)f2bf(v[8 * c + 3]) << 16);
-    q.z = (uint32_t)f2bf(v[8 * c + 4]) | ((uint32_t)f2bf(v[8 * c + 5]) << 16);
-    q.w = (uint32_t)f2bf(v[8 * c + 6]) | ((uint32_t)f2bf(v[8 * c + 7]) << 16);
-    *(uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4)) = q;
-  }
-}
-
-__device__ __forceinline__ void load_row_bf16(const uint8_t* tile, int row, float* v) {
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const uint4 q = *(const uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4));
-    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      v[8 * c + 2 * j] = bf2f((uint16_t)(w[j] & 0xffffu));
-      v[8 * c + 2 * j + 1] = bf2f((uint16_t)(w[j] >> 16));
-    }
-  }
-}
-
-// D = A(128 x 64) * B(N x 64)^T: four K = 16 steps, then a commit.
-__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* a, const uint8_t* b, uint32_t N,
-                                            uint64_t* mbar) {
-  const uint32_t sa = tc::smem_u32(a), sb = tc::smem_u32(b);
-  const uint32_t idesc = tc::idesc_bf16_f32(128, N);
-#pragma unroll
-  for (uint32_t k = 0; k < 4; ++k) tc::mma_bf16(d_tmem, tc::sw128_desc(sa + 32 * k), tc::sw128_desc(sb + 32 * k), idesc, k);
-  tc::mma_commit(mbar);
-}
-
-__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
-  return (uint8_t*)(((uintptr_t)p + 1023) & ~(uintptr_t)1023);
-}
-
 // ---------------------------------------------------------------------------------
 // inference: out[i][0..39] = network(features_i)
 
-// + 1024 for the manual 1024-byte alignment, + 16 KB of slack after the last
-// operand tile
-constexpr int INFER_SMEM = FWD_BYTES + 2 * 16384 + 1024 + 16384;
-
 template <int SRC>
-__global__ void __launch_bounds__(128, 1) k_guide_infer(const uint16_t* __restrict__ pack, const float* __restrict__ master,
-                                                        GuideSrc src, float* __restrict__ out, uint32_t* status) {
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = align1024(smem_raw);
-  uint8_t* w = smem;
-  uint8_t* act[2] = {smem + FWD_BYTES, smem + FWD_BYTES + 16384};
-  __shared__ uint64_t mbar;
-  __shared__ uint32_t tmem_base;
-  __shared__ int failed;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  // samples [src.first, n)
-  const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
-  const uint32_t ntiles = (n - src.first + 127) / 128;
-  if (blockIdx.x >= ntiles) return;
-  if (tid == 0) {
-    tc::mbar_init(&mbar, 1);
-    failed = 0;
-  }
-  if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
-  for (int c = tid; c < FWD_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
-  tc::fence_smem_async();
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_base;
-  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  uint32_t phase = 0;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint32_t i = src.first + t * 128 + tid;
-    float f[64];
-    if (i < n) load_features<SRC>(src, i, f);
-    else
+__global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guide_infer(const uint16_t* __restrict__ pack,
+                                                                          const float* __restrict__ master,
+                                                                          GuideSrc src, float* __restrict__ out,
+                                                                          uint32_t* status) {
+  infer_tiles<SRC>(pack, master, src, status, [&](uint32_t i, bool valid, const float* o) {
+    if (!valid) return;
+    float4* d = reinterpret_cast<float4*>(out + 40ull * i);
 #pragma unroll
-      for (int k = 0; k < 64; ++k) f[k] = 0.0f;
-    store_row_bf16(act[0], tid, f);
-    int cur = 0;
-    for (int l = 0; l < 5; ++l) {
-      tc::fence_smem_async();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      const uint32_t N = l < 4 ? 64u : 48u;
-      if (tid == 0) issue_layer(tmem, act[cur], w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, N, &mbar);
-      if (!tc::mbar_wait(&mbar, phase)) {
-        atomicOr(status, ST_GUIDE_NONFINITE << 1);
-        failed = 1;
-      }
-      phase ^= 1;
-      tc::fence_after_sync();
-      __syncthreads();
-      if (failed) break;
-      float acc[64];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        if (c * 16 < (int)N) tc::tmem_ld16(lane_addr + c * 16, acc + c * 16);
-      }
-      if (l < 4) {
-        const float* b = master + P_B + 64 * l;
-#pragma unroll
-        for (int k = 0; k < 64; ++k) acc[k] = fmaxf(acc[k] + __ldg(b + k), 0.0f);
-        store_row_bf16(act[cur ^ 1], tid, acc);
-        cur ^= 1;
-      } else if (i < n) {
-        float4* o = (float4*)(out + 40ull * i);
-#pragma unroll
-        for (int k = 0; k < 10; ++k)
-          o[k] = make_float4(acc[4 * k] + __ldg(master + P_B5 + 4 * k), acc[4 * k + 1] + __ldg(master + P_B5 + 4 * k + 1),
-                             acc[4 * k + 2] + __ldg(master + P_B5 + 4 * k + 2),
-                             acc[4 * k + 3] + __ldg(master + P_B5 + 4 * k + 3));
-      }
-      tc::fence_before_sync();
-    }
-    if (failed) break;
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+    for (int k = 0; k < 10; ++k) d[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+  });
 }
 
 // ---------------------------------------------------------------------------------
@@ -578,7 +421,7 @@ static int sm_count_current() {
 
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n, cudaStream_t s) {
   const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
-  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
+  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current() * INFER_BLOCKS_PER_SM);
   if (src_kind == SRC_RAW)
     k_guide_infer<SRC_RAW><<<grid, 128, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
   else
@@ -645,8 +488,10 @@ Status guide_renderer_init(Renderer& r) {
     r.scenes[s].guide = (int)s;
     r.guides.push_back(std::move(g));
   }
-  LISA_TRY(r.arena.alloc((void**)&r.guide_out, sizeof(float) * 40ull * r.capacity, "guide outputs"));
+  LISA_TRY(guided_infer_setup());
   LISA_TRY(r.arena.alloc((void**)&r.train_rec, sizeof(float4) * 5ull * maxd * r.capacity, "guide records"));
+  if (r.opts.estimator == LISA_ESTIMATOR_PHYSICAL)
+    LISA_TRY(r.arena.alloc((void**)&r.nee_light, sizeof(float4) * 2ull * r.capacity, "emitter samples"));
   LISA_TRY(r.arena.alloc((void**)&r.guide_batch, sizeof(float4) * 4ull * B, "guide batch"));
   return Status();
 }

@@ -45,6 +45,7 @@ struct GuideSrc {
   const uint32_t* count;  // device sample count, clamped to n; null: use n
   uint32_t n;             // samples [first, min(count, n)) are used
   uint32_t first;
+  uint32_t no_flag;       // SRC_NEE: the emitter-flag feature is 0 (physically based estimator)
   float bmin[3], bmax[3];
 };
 
@@ -65,6 +66,8 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float 
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s);
 Status guide_check_status(GuideNet& g, cudaStream_t s);
 Status guide_renderer_init(Renderer& r);
+// Shared-memory attributes of the renderer's fused inference kernels (wavefront.cu).
+Status guided_infer_setup();
 
 }  // namespace lisa
 

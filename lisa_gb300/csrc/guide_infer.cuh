@@ -1,0 +1,220 @@
+// Inference core of the guide network, shared by the standalone inference
+// kernel (guide.cu) and the renderer's fused inference + guided-bounce
+// kernels (wavefront.cu): parameter and packed-weight layouts, feature
+// loading, and infer_tiles(), which runs the five layers on the tensor cores
+// tile by tile and hands each thread its sample's 40 outputs.
+//
+// Network: 64 encoded inputs -> 4 x (64, ReLU) -> 40 outputs = 8 vMF lobes
+// (guide_mix.cuh).  A CTA of 128 threads processes tiles of 128 samples:
+// thread t owns row t of every activation tile and TMEM lane t of the
+// accumulator.  One thread issues tcgen05.mma (M = 128, K = 16 per
+// instruction), commits to an mbarrier and waits (bounded; a time-out sets a
+// status bit), the block meets at a barrier, then every thread reads its
+// accumulator row with tcgen05.ld.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "guide.cuh"
+#include "guide_mix.cuh"
+#include "lisa_device.cuh"
+#include "tcgen05.cuh"
+
+namespace lisa {
+
+// ---- parameter layout (FP32 master) ------------------------------------------
+constexpr int P_W = 0;                    // W1..W4: 4 x 64 x 64, then W5: 40 x 64
+constexpr int P_W5 = 4 * 64 * 64;
+constexpr int P_B = P_W5 + 40 * 64;       // b1..b4: 4 x 64, then b5: 40
+constexpr int P_B5 = P_B + 4 * 64;
+constexpr int NPARAM = P_B5 + 40;
+static_assert(NPARAM == LISA_GUIDE_NUM_PARAMS, "parameter count");
+
+// ---- packed BF16 weights: rows of 128 B, pre-swizzled in 8-row groups ------------
+constexpr int R_FWD = 0;        // W1..W4 forward: 4 x 64 rows (row = output)
+constexpr int R_W5 = 256;       // W5 forward: 48 rows (40 used)
+constexpr int R_T = 304;        // W2^T..W5^T: 4 x 64 rows (row = input, K = output)
+constexpr int R_TOTAL = 560;
+constexpr int PACK_BYTES = R_TOTAL * 128;
+constexpr int FWD_BYTES = R_T * 128;  // what inference needs
+
+__device__ __forceinline__ uint16_t f2bf(float x) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+__device__ __forceinline__ float bf2f(uint16_t h) { return __bfloat162float(__ushort_as_bfloat16(h)); }
+
+template <int SRC>
+__device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, float* f) {
+  if (SRC == SRC_RAW) {
+    const float4* r = (const float4*)(s.raw + 64ull * i);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const float4 x = __ldg(r + c);
+      f[4 * c] = x.x;
+      f[4 * c + 1] = x.y;
+      f[4 * c + 2] = x.z;
+      f[4 * c + 3] = x.w;
+    }
+  } else if (SRC == SRC_GEOM) {
+    const float4 a = s.geom[4ull * i], b = s.geom[4ull * i + 1], c = s.geom[4ull * i + 2], d = s.geom[4ull * i + 3];
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, d.y, f);
+  } else {
+    const float4 a = s.nee_a[i], b = s.nee_b[i], c = s.nee_c[i];
+    // view direction: towards where the ray came from
+    const float il = rsqrtf(fmaxf(c.x * c.x + c.y * c.y + c.z * c.z, 1e-30f));
+    const int stale = __float_as_int(s.ps_att[__float_as_uint(a.w)].w);
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il,
+                  (stale >= 0 && !s.no_flag) ? 1.0f : 0.0f, f);
+  }
+}
+
+// Writes 64 values as BF16 (round to nearest even) into row `row` of a
+// swizzled tile, two values per conversion.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);  // .x (low half) = lo
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ void store_row_bf16(uint8_t* tile, int row, const float* v) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    uint4 q;
+    q.x = pack_bf16x2(v[8 * c + 0], v[8 * c + 1]);
+    q.y = pack_bf16x2(v[8 * c + 2], v[8 * c + 3]);
+    q.z = pack_bf16x2(v[8 * c + 4], v[8 * c + 5]);
+    q.w = pack_bf16x2(v[8 * c + 6], v[8 * c + 7]);
+    *(uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4)) = q;
+  }
+}
+
+__device__ __forceinline__ void load_row_bf16(const uint8_t* tile, int row, float* v) {
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const uint4 q = *(const uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4));
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      v[8 * c + 2 * j] = bf2f((uint16_t)(w[j] & 0xffffu));
+      v[8 * c + 2 * j + 1] = bf2f((uint16_t)(w[j] >> 16));
+    }
+  }
+}
+
+// D = A(128 x 64) * B(N x 64)^T: four K = 16 steps, then a commit.
+__device__ __forceinline__ void issue_layer(uint32_t d_tmem, const uint8_t* a, const uint8_t* b, uint32_t N,
+                                            uint64_t* mbar) {
+  const uint32_t sa = tc::smem_u32(a), sb = tc::smem_u32(b);
+  const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) tc::mma_bf16(d_tmem, tc::sw128_desc(sa + 32 * k), tc::sw128_desc(sb + 32 * k), idesc, k);
+  tc::mma_commit(mbar);
+}
+
+__device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
+  return (uint8_t*)(((uintptr_t)p + 1023) & ~(uintptr_t)1023);
+}
+
+// ---------------------------------------------------------------------------------
+// inference: the five layers, tile by tile
+
+// + 1024 for the manual 1024-byte alignment, + 2 KB of slack after the last
+// operand tile.  Three CTAs share an SM (3 x 75.8 KB of shared memory,
+// 3 x 64 TMEM columns, <= 168 registers a thread), so one CTA's tensor-core
+// waits and TMEM round trips overlap the others' epilogues.
+constexpr int INFER_SMEM = FWD_BYTES + 2 * 16384 + 1024 + 2048;
+constexpr int INFER_BLOCKS_PER_SM = 3;
+
+// Runs the network on samples [src.first, n) and calls
+// epi(i, valid, o) in every thread for its sample i of each tile (valid =
+// i < n; o = the 40 outputs, bias included).  All 128 threads call epi
+// together, so it may use warp-collective operations.  Needs INFER_SMEM
+// bytes of dynamic shared memory and 128 threads.
+template <int SRC, class Epi>
+__device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, const float* __restrict__ master,
+                                            const GuideSrc& src, uint32_t* status, Epi&& epi) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* w = smem;
+  uint8_t* act[2] = {smem + FWD_BYTES, smem + FWD_BYTES + 16384};
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int failed;
+  __shared__ __align__(16) float s_bias[4 * 64 + 48];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // samples [src.first, n)
+  const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
+  const uint32_t ntiles = (n - src.first + 127) / 128;
+  if (blockIdx.x >= ntiles) return;
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    failed = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+  for (int c = tid; c < FWD_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
+  for (int k = tid; k < 4 * 64 + 48; k += 128) s_bias[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
+  tc::fence_smem_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t i = src.first + t * 128 + tid;
+    {
+      float f[64];
+      if (i < n) load_features<SRC>(src, i, f);
+      else
+#pragma unroll
+        for (int k = 0; k < 64; ++k) f[k] = 0.0f;
+      store_row_bf16(act[0], tid, f);
+    }
+    int cur = 0;
+#pragma unroll 1
+    for (int l = 0; l < 5; ++l) {
+      tc::fence_smem_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      if (tid == 0) {
+        issue_layer(tmem, act[cur], w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, l < 4 ? 64u : 48u, &mbar);
+        if (!tc::mbar_wait(&mbar, phase)) {
+          atomicOr(status, ST_GUIDE_NONFINITE << 1);
+          failed = 1;
+        }
+      }
+      phase ^= 1;
+      __syncthreads();  // the others learn of the finished MMA here
+      tc::fence_after_sync();
+      if (failed) break;
+      float acc[64];
+      if (l < 4) {
+        tc::tmem_ld16x<4>(lane_addr, acc);
+        const float4* bb = reinterpret_cast<const float4*>(s_bias + 64 * l);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const float4 b4 = bb[k];
+          acc[4 * k] = fmaxf(acc[4 * k] + b4.x, 0.0f);
+          acc[4 * k + 1] = fmaxf(acc[4 * k + 1] + b4.y, 0.0f);
+          acc[4 * k + 2] = fmaxf(acc[4 * k + 2] + b4.z, 0.0f);
+          acc[4 * k + 3] = fmaxf(acc[4 * k + 3] + b4.w, 0.0f);
+        }
+        store_row_bf16(act[cur ^ 1], tid, acc);
+        cur ^= 1;
+      } else {
+        tc::tmem_ld16x<3>(lane_addr, acc);
+#pragma unroll
+        for (int k = 0; k < 40; ++k) acc[k] += s_bias[4 * 64 + k];
+        epi(i, i < n, acc);
+      }
+      tc::fence_before_sync();
+    }
+    if (failed) break;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+}  // namespace lisa

@@ -35,7 +35,8 @@ struct DevMaterial {
   float ior;
   int cls;
   float alpha;
-  int pad[2];
+  float light_pdf;  // physically based estimator: area pdf (luminance / total) of its emitters
+  int pad;
 };
 static_assert(sizeof(DevMaterial) == 48, "DevMaterial layout");
 
@@ -76,6 +77,13 @@ struct SceneDev {
   uint32_t* pix_rng; // reference per-pixel stream state (LISA_RNG_PER_PIXEL)
   int32_t guide;     // guide slot of this scene (-1 = none)
   int32_t pad1;
+  // physically based estimator: emitters, 4 float4 each --
+  // (v0.xyz, area pdf) (e1 = v1-v0, material bits) (e2 = v2-v0, 0) (unit normal, 0)
+  // -- and the CDF over area x luminance that picks them
+  const float4* emit;
+  const float* emit_cdf;
+  uint32_t num_emit;
+  uint32_t pad2;
 };
 
 // One group of a wave: `nplanes` consecutive sample planes of pixels

@@ -141,6 +141,9 @@ struct SceneGpu {
   double* acc_sq = nullptr;
   double* acc_sum64 = nullptr;
   uint32_t* pix_rng = nullptr;
+  float4* emit = nullptr;       // physically based estimator: emitter records
+  float* emit_cdf = nullptr;
+  uint32_t num_emit = 0;
   float extent = 0.0f;
   float eye[3], U[3], V[3], W[3];
   int guide = -1;
@@ -183,8 +186,8 @@ struct Renderer {
   uint32_t graph_launches[5] = {0, 0, 0, 0, 0};  // trace, shade, nee, total, guide
   // guided mode
   std::vector<std::unique_ptr<GuideNet>> guides;
-  float* guide_out = nullptr;    // capacity x 40 network outputs
   float4* train_rec = nullptr;   // capacity x max_depth x 5 training records
+  float4* nee_light = nullptr;   // guided physically based mode: capacity x 2 emitter samples
   float4* guide_batch = nullptr; // guide_batch_cap x 4 training samples
   uint32_t guide_batch_cap = 0;  // samples collected per wave
   uint32_t guide_chunk = 0;      // samples per Adam step

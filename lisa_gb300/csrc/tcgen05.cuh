@@ -119,5 +119,33 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// CH x 16 consecutive FP32 columns of this thread's TMEM lane: all loads
+// issued, then one wait.
+template <int CH>
+__device__ __forceinline__ void tmem_ld16x(uint32_t taddr, float* v) {
+  uint32_t r[CH][16];
+#pragma unroll
+  for (int c = 0; c < CH; ++c)
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[c][0]), "=r"(r[c][1]), "=r"(r[c][2]), "=r"(r[c][3]), "=r"(r[c][4]), "=r"(r[c][5]), "=r"(r[c][6]),
+          "=r"(r[c][7]), "=r"(r[c][8]), "=r"(r[c][9]), "=r"(r[c][10]), "=r"(r[c][11]), "=r"(r[c][12]),
+          "=r"(r[c][13]), "=r"(r[c][14]), "=r"(r[c][15])
+        : "r"(taddr + 16u * c));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  // The loaded registers may be read only after the wait: an empty volatile
+  // statement that "modifies" them keeps every use below it.
+#pragma unroll
+  for (int c = 0; c < CH; ++c)
+    asm volatile(""
+                 : "+r"(r[c][0]), "+r"(r[c][1]), "+r"(r[c][2]), "+r"(r[c][3]), "+r"(r[c][4]), "+r"(r[c][5]),
+                   "+r"(r[c][6]), "+r"(r[c][7]), "+r"(r[c][8]), "+r"(r[c][9]), "+r"(r[c][10]), "+r"(r[c][11]),
+                   "+r"(r[c][12]), "+r"(r[c][13]), "+r"(r[c][14]), "+r"(r[c][15]));
+#pragma unroll
+  for (int c = 0; c < CH; ++c)
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[16 * c + i] = __uint_as_float(r[c][i]);
+}
+
 }  // namespace tc
 }  // namespace lisa

@@ -30,6 +30,8 @@
 #define LISA_BSDF_HEADER "bsdfs/lambertian.cuh"
 #endif
 #include LISA_BSDF_HEADER
+#include "guide_infer.cuh"
+#include "physical.cuh"
 
 namespace lisa {
 
@@ -157,7 +159,9 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
     }
     b.ro[0][slot] = make_float4(org.x, org.y, org.z, __uint_as_float(slot));
     b.rd[0][slot] = make_float4(dir.x, dir.y, dir.z, RAY_TMAX);
-    b.ps_att[slot] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(-1));
+    // w: the stale emitter flag (compat, -1 = none) or the pdf of the last
+    // diffuse bounce (physically based, 0 = camera or specular)
+    b.ps_att[slot] = make_float4(1.0f, 1.0f, 1.0f, b.physical ? 0.0f : __int_as_float(-1));
     b.ps_col[slot] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float((g.scene << 24) | pix));
     b.ps_rng[slot] = seed;
     if (b.train_rec)  // guided mode: no training record yet at any depth
@@ -229,6 +233,7 @@ __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
 // ---------------------------------------------------------------------------
 // shade: emitter / miss / dielectric / opaque (shader.cu:189-194,211-255)
 
+template <bool PHYS>
 __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->qcount[q];
@@ -255,7 +260,25 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
         float4 att = b.ps_att[slot];
         if (m.cls == MAT_EMIT) {
           // color += Le * att; done (shader.cu:216-218)
-          const V3 c = ld3(col) + v3(m.emission[0], m.emission[1], m.emission[2]) * ld3(att);
+          V3 le = v3(m.emission[0], m.emission[1], m.emission[2]) * ld3(att);
+          if (PHYS && att.w > 0.0f) {
+            // reached by a diffuse bounce: power-heuristic weight against
+            // the emitter sampler's density for this direction
+            const float prev = att.w;
+            const float t = __int_as_float(h.y);
+            const float4* pr = sc.prims + 5ull * h.x;
+            const V3 v0 = ld3(pr[0]);
+            const V3 cr = cross3(ld3(pr[1]) - v0, ld3(pr[2]) - v0);
+            const V3 n = cr * fdiv(1.0f, fsqrt(dot(cr, cr)));
+            const float cos_y = fabsf(dot(n, ld3(b.rd[q][i])));
+            float w = 0.0f;
+            if (cos_y > 0.0f) {
+              const float pl = fdiv(fmul(m.light_pdf, fmul(t, t)), cos_y);
+              w = fdiv(fmul(prev, prev), fadd(fmul(prev, prev), fmul(pl, pl)));
+            }
+            le = le * w;
+          }
+          const V3 c = ld3(col) + le;
           b.ps_col[slot] = make_float4(c.x, c.y, c.z, col.w);
         } else {
           const float4 d4 = b.rd[q][i];
@@ -281,6 +304,17 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
             uint32_t seed = b.ps_rng[slot];
             if (eta == 1.0f) {
               nd = d;
+            } else if (PHYS) {
+              // total internal reflection reflects; Schlick's term takes the
+              // cosine on the less dense side (the transmitted one on exit)
+              const float cost2 = fsub(1.0f, fmul(fmul(eta, eta), fsub(1.0f, fmul(cosI, cosI))));
+              if (cost2 <= 0.0f) {
+                nd = reflect(d, nrm);
+              } else if (rnd(seed) <= bsdf::BTDF(eta > 1.0f ? fsqrt(cost2) : cosI, eta)) {
+                nd = reflect(d, nrm);
+              } else {
+                nd = bsdf::refract(cosI, d, nrm, eta);
+              }
             } else if (rnd(seed) <= bsdf::BTDF(cosI, eta)) {
               nd = reflect(d, nrm);
             } else {
@@ -288,7 +322,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
               nd = bsdf::refract(cosI, d, nrm, eta);
             }
             b.ps_rng[slot] = seed;
-            b.ps_att[slot] = make_float4(a.x, a.y, a.z, att.w);
+            b.ps_att[slot] = make_float4(a.x, a.y, a.z, PHYS ? 0.0f : att.w);
             want_ray = !last && !is_zero(nd);
           } else {
             const V3 a = ld3(att) * v3(m.albedo[0], m.albedo[1], m.albedo[2]);
@@ -328,12 +362,9 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
 // (probability c) and the guide's vMF mixture.  The path continues with
 // weight p_hemi(w) / (c p_hemi(w) + (1-c) q_guide(w)), so the estimator's
 // expectation is unchanged; directions below the surface get weight 0.
-__device__ __forceinline__ V3 guided_bounce(const float* __restrict__ o, V3 N, uint32_t& seed, float c, float& weight) {
+__device__ __forceinline__ V3 guided_bounce(const float* o, V3 N, uint32_t& seed, float c, float& weight) {
   guide::Lobe L[guide::LOBES];
-  float raw[guide::NOUT];
-#pragma unroll
-  for (int k = 0; k < guide::NOUT; ++k) raw[k] = __ldg(o + k);
-  guide::decode(raw, L);
+  guide::decode(o, L);
   V3 w;
   if (rnd(seed) < c) {
     w = bsdf::shoot_ray_hemisphere(N, seed);
@@ -395,7 +426,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
             b.ps_col[slot] = make_float4(col.x, col.y, col.z, c.w);
           }
           if (GUIDED && sc->mats[mat_idx].roughness == 1.0f) {
-            // the bounce of a guided vertex is drawn by k_guided_bounce,
+            // the bounce of a guided vertex is drawn by k_guided_infer,
             // after the guide has seen the emitter flag this search left
             want_ray = false;
           } else {
@@ -468,58 +499,278 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
 }
 
 // ---------------------------------------------------------------------------
-// guided bounce of the opaque vertices with roughness 1 (deferred by k_nee
-// until the guide's inference has run on the post-search state), with a
-// training record per vertex: the radiance later gathered along the new
-// direction, over the throughput after the bounce, is the incident radiance.
+// Guided bounces, in the epilogue of the guide's inference (k_guided_infer):
+// thread t holds the 40 network outputs of emitter-queue entry i in
+// registers and finishes that vertex, so the outputs never reach HBM.
+//
+// Reference estimator: the opaque vertices with roughness 1, whose bounce
+// k_nee deferred until the guide had seen the emitter flag its search left,
+// with a training record per vertex (the radiance later gathered along the
+// new direction, over the throughput after the bounce, is the incident
+// radiance).  Returns whether a continuation ray (p, nd) is wanted.
+__device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int depth, uint32_t i, const float* o, V3& p,
+                                                     V3& nd, uint32_t& slot, uint32_t& guided_n) {
+  const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
+  slot = __float_as_uint(a4.w);
+  const float4 cw = b.ps_col[slot];
+  const SceneDev& sc = b.scenes[__float_as_uint(cw.w) >> 24];
+  if (sc.mats[__float_as_int(b4.w)].roughness != 1.0f) return false;  // bounced in k_nee
+  p = ld3(a4);
+  const V3 N = ld3(b4);
+  const V3 D = ld3(b.nee_c[i]);
+  uint32_t seed = b.ps_rng[slot];
+  const float4 at = b.ps_att[slot];
+  const int stale = __float_as_int(at.w);
+  float weight;
+  nd = guided_bounce(o, N, seed, b.bsdf_fraction, weight);
+  const V3 att = ld3(at) * weight;
+  const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
+  float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + depth);
+  rec[0] = make_float4(p.x, p.y, p.z, weight);
+  rec[1] = make_float4(N.x, N.y, N.z, nd.x);
+  rec[2] = make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y);
+  rec[3] = make_float4(att.x, att.y, att.z, nd.z);
+  rec[4] = make_float4(cw.x, cw.y, cw.z, stale >= 0 ? 2.0f : 1.0f);  // 0 = no record
+  b.ps_rng[slot] = seed;
+  b.ps_att[slot] = make_float4(att.x, att.y, att.z, at.w);
+  ++guided_n;
+  return depth + 1 < (int)sc.num_bounces && weight > 0.0f;
+}
 
-__global__ void __launch_bounds__(256) k_guided_bounce(WaveBufs b, int depth) {
+// ---------------------------------------------------------------------------
+// physically based estimator at opaque vertices (opt-in; no reference
+// counterpart).  Emitter sampling: one shadow ray toward a point of an
+// emitter picked by area x luminance (two-sided emitters), weighted against
+// the bounce's density by the power heuristic.  Bounce: the diffuse lobe
+// with probability = roughness (cosine-weighted), else a mirror; the
+// throughput keeps the albedo applied by k_shade.  ps_att.w carries the
+// solid-angle density of the last diffuse bounce (0 after a camera ray or a
+// specular event) for the weight at an emitter hit (k_shade<true>).
+//
+// Plain mode finishes each vertex here.  Guided mode (SPLIT) only traces the
+// shadow ray and leaves (direction, density, cosine, emitter material,
+// visibility) in nee_light; k_guided_infer weighs it with the guide's density
+// and draws the bounce once the guide's inference has run.
+
+template <bool COUNT, bool SPLIT>
+__global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee_pb(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->nee_count;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  const uint32_t lt = lanemask_lt();
+  uint2 stack[TRAV_STACK];
+  TravState s;
+  TraceScene ts;
+  const SceneDev* sc = nullptr;
+  bool have = false, exhausted = false, ray_active = false, pending = false, shadow = false;
+  uint32_t entry = 0, slot = 0, seed = 0;
+  int mat_idx = 0, em_m = 0;
+  V3 Ns = v3(0.0f), wi = v3(0.0f);  // the vertex position lives in s.r.o*
+  float pl = 0.0f, cos_x = 0.0f;
+  s.r.ox = s.r.oy = s.r.oz = 0.0f;
+  uint32_t nshadow = 0, visits = 0, tests = 0;
+  while (true) {
+    const uint32_t busy = __ballot_sync(FULL, ray_active);
+    if (__popc(busy) <= (int)b.refill_busy_max) {
+      bool want_ray = false;
+      V3 nd = v3(0.0f);
+      if (pending) {
+        pending = false;
+        const bool lit = shadow && s.best_prim < 0;
+        if (SPLIT) {
+          b.nee_light[2ull * entry] = make_float4(wi.x, wi.y, wi.z, pl);
+          b.nee_light[2ull * entry + 1] = make_float4(cos_x, __int_as_float(em_m), lit ? 1.0f : 0.0f, 0.0f);
+          b.ps_rng[slot] = seed;
+        } else {
+          const DevMaterial& m = sc->mats[mat_idx];
+          const float r = m.roughness;
+          const float4 at = b.ps_att[slot];
+          const V3 att = ld3(at);
+          if (lit) {
+            const DevMaterial& em = sc->mats[em_m];
+            const float fcos = fmul(r, fdiv(cos_x, PI_F));
+            const float wl = fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(fcos, fcos)));
+            const float4 c = b.ps_col[slot];
+            const V3 col =
+                ld3(c) + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
+            b.ps_col[slot] = make_float4(col.x, col.y, col.z, c.w);
+          }
+          float prev = 0.0f;
+          if (r >= 1.0f || (r > 0.0f && rnd(seed) < r)) {
+            nd = cosine_dir(Ns, seed);
+            prev = fmul(r, fdiv(dot(Ns, nd), PI_F));
+          } else {
+            nd = reflect(ld3(b.nee_c[entry]), Ns);
+          }
+          want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
+          b.ps_rng[slot] = seed;
+          b.ps_att[slot] = make_float4(att.x, att.y, att.z, prev);
+        }
+        have = false;
+      }
+      const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
+      if (want_ray) {
+        b.ro[q ^ 1][ri] = make_float4(s.r.ox, s.r.oy, s.r.oz, __uint_as_float(slot));
+        b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+      }
+      const bool need = !have && !exhausted;
+      const uint32_t nmask = __ballot_sync(FULL, need);
+      if (nmask) {
+        const int leader = __ffs(nmask) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&b.ctrl->head[HEAD_NEE], (uint32_t)__popc(nmask));
+        base = __shfl_sync(FULL, base, leader);
+        if (need) {
+          entry = base + __popc(nmask & lt);
+          if (entry < count) {
+            const float4 a4 = b.nee_a[entry], b4 = b.nee_b[entry];
+            const V3 p = ld3(a4);
+            s.r.ox = p.x;
+            s.r.oy = p.y;
+            s.r.oz = p.z;
+            slot = __float_as_uint(a4.w);
+            const V3 N = ld3(b4);
+            mat_idx = __float_as_int(b4.w);
+            seed = b.ps_rng[slot];
+            sc = b.scenes + (__float_as_uint(b.ps_col[slot].w) >> 24);
+            ts = trace_scene(*sc);
+            Ns = dot(N, ld3(b.nee_c[entry])) < 0.0f ? N : -N;  // faces the incoming ray
+            have = true;
+            shadow = false;
+            wi = v3(0.0f);
+            pl = cos_x = 0.0f;
+            em_m = 0;
+            if (sc->mats[mat_idx].roughness > 0.0f && sc->num_emit > 0) {
+              V3 y;
+              const uint32_t k = sample_emitter(*sc, seed, y);
+              const V3 w = y - p;
+              const float d2 = dot(w, w);
+              const float dist = fsqrt(d2);
+              wi = w * fdiv(1.0f, dist);
+              cos_x = dot(Ns, wi);
+              const float cos_y = fabsf(dot(ld3(__ldg(sc->emit + 4ull * k + 3)), wi));
+              if (cos_x > 0.0f && cos_y > 0.0f && dist > 0.0f) {
+                pl = fdiv(fmul(__ldg(sc->emit + 4ull * k).w, d2), cos_y);
+                em_m = __float_as_int(__ldg(sc->emit + 4ull * k + 1).w);
+                shadow = true;
+                ++nshadow;
+                // stop short of the emitter itself
+                ray_active = trav_begin(s, ts, p, wi, RAY_TMIN, fmul(dist, 0.9990234375f));
+              }
+            }
+            pending = !ray_active;  // no shadow ray, or nothing to traverse
+          } else {
+            exhausted = true;
+          }
+        }
+      }
+      if (!__any_sync(FULL, have)) break;
+    }
+    if (ray_active && trav_step<COUNT>(s, ts, stack, visits, tests, &b.ctrl->status)) {
+      ray_active = false;
+      pending = true;
+    }
+  }
+  warp_add64(&b.ctrl->rays_shadow, nshadow);
+  if (COUNT) {
+    warp_add64(&b.ctrl->node_visits[1], visits);
+    warp_add64(&b.ctrl->tri_tests[1], tests);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    b.ctrl->head[HEAD_TRACE] = 0;
+    b.ctrl->nee_total += count;
+  }
+}
+
+// Physically based estimator: the emitter sample of k_nee_pb weighed
+// against the guided density, then the bounce -- the diffuse lobe by
+// one-sample MIS between cosine sampling (probability c) and the guide's
+// mixture, q = c cos/pi + (1-c) q_guide, throughput x (cos/pi) / q -- with a
+// training record per diffuse bounce.
+__device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, uint32_t i, const float* o, V3& p,
+                                                 V3& nd, uint32_t& slot, uint32_t& guided_n) {
+  const float c = b.bsdf_fraction;
+  const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
+  p = ld3(a4);
+  slot = __float_as_uint(a4.w);
+  const V3 N = ld3(b4);
+  const V3 D = ld3(b.nee_c[i]);
+  const V3 Ns = dot(N, D) < 0.0f ? N : -N;
+  const float4 cw = b.ps_col[slot];
+  const SceneDev& sc = b.scenes[__float_as_uint(cw.w) >> 24];
+  const float r = sc.mats[__float_as_int(b4.w)].roughness;
+  V3 att = ld3(b.ps_att[slot]);
+  V3 col = ld3(cw);
+  uint32_t seed = b.ps_rng[slot];
+  guide::Lobe L[guide::LOBES];
+  guide::decode(o, L);
+  const float4 l0 = b.nee_light[2ull * i], l1 = b.nee_light[2ull * i + 1];
+  if (l1.z != 0.0f) {
+    const float pl = l0.w, cos_x = l1.x;
+    const DevMaterial& em = sc.mats[__float_as_int(l1.y)];
+    const float fcos = fmul(r, fdiv(cos_x, PI_F));
+    const float pb = r * (c * (cos_x / PI_F) + (1.0f - c) * guide::mix_pdf(L, l0.x, l0.y, l0.z));
+    const float wl = (pl * pl) / (pl * pl + pb * pb);
+    col = col + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
+  }
+  float prev = 0.0f;
+  bool want;
+  if (r >= 1.0f || (r > 0.0f && rnd(seed) < r)) {
+    if (rnd(seed) < c) {
+      nd = cosine_dir(Ns, seed);
+    } else {
+      const float u0 = rnd(seed), u1 = rnd(seed), u2 = rnd(seed);
+      guide::mix_sample(L, u0, u1, u2, nd.x, nd.y, nd.z);
+    }
+    const float cs = dot(Ns, nd);
+    const float pc = cs > 0.0f ? cs / PI_F : 0.0f;
+    const float qm = c * pc + (1.0f - c) * guide::mix_pdf(L, nd.x, nd.y, nd.z);
+    const float weight = (pc > 0.0f && qm > 0.0f && isfinite(qm)) ? pc / qm : 0.0f;
+    att = att * weight;
+    prev = r * qm;
+    want = depth + 1 < (int)sc.num_bounces && weight > 0.0f;
+    const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
+    float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + depth);
+    rec[0] = make_float4(p.x, p.y, p.z, weight);
+    rec[1] = make_float4(N.x, N.y, N.z, nd.x);
+    rec[2] = make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y);
+    rec[3] = make_float4(att.x, att.y, att.z, nd.z);
+    rec[4] = make_float4(col.x, col.y, col.z, 1.0f);  // flag feature 0
+    ++guided_n;
+  } else {
+    nd = reflect(D, Ns);
+    want = depth + 1 < (int)sc.num_bounces;
+  }
+  b.ps_col[slot] = make_float4(col.x, col.y, col.z, cw.w);
+  b.ps_rng[slot] = seed;
+  b.ps_att[slot] = make_float4(att.x, att.y, att.z, prev);
+  return want;
+}
+
+// The guide's inference on the emitter queue of this depth, fused with the
+// guided bounces of those vertices (tensor-core layers, guide_infer.cuh;
+// bounce in the last layer's epilogue).
+template <bool PHYS>
+__global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const uint16_t* __restrict__ pack,
+                                                                           const float* __restrict__ master,
+                                                                           GuideSrc src, uint32_t* status, WaveBufs b,
+                                                                           int depth) {
+  const int q = depth & 1;
   uint32_t guided_n = 0;
-  for (uint32_t base = gw * 32; base < count; base += warps * 32) {
-    const uint32_t i = base + lane;
+  infer_tiles<SRC_NEE>(pack, master, src, status, [&](uint32_t i, bool valid, const float* o) {
     bool want = false;
     V3 p = v3(0.0f), nd = v3(0.0f);
     uint32_t slot = 0;
-    if (i < count) {
-      const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
-      slot = __float_as_uint(a4.w);
-      const float4 cw = b.ps_col[slot];
-      const SceneDev& sc = b.scenes[__float_as_uint(cw.w) >> 24];
-      const int mat = __float_as_int(b4.w);
-      if (sc.mats[mat].roughness == 1.0f) {
-        p = ld3(a4);
-        const V3 N = ld3(b4);
-        const V3 D = ld3(b.nee_c[i]);
-        uint32_t seed = b.ps_rng[slot];
-        const float4 at = b.ps_att[slot];
-        const int stale = __float_as_int(at.w);
-        float weight;
-        nd = guided_bounce(b.guide_out + 40ull * i, N, seed, b.bsdf_fraction, weight);
-        const V3 att = ld3(at) * weight;
-        want = depth + 1 < (int)sc.num_bounces && weight > 0.0f;
-        const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-        float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + depth);
-        rec[0] = make_float4(p.x, p.y, p.z, weight);
-        rec[1] = make_float4(N.x, N.y, N.z, nd.x);
-        rec[2] = make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y);
-        rec[3] = make_float4(att.x, att.y, att.z, nd.z);
-        rec[4] = make_float4(cw.x, cw.y, cw.z, stale >= 0 ? 2.0f : 1.0f);  // 0 = no record
-        b.ps_rng[slot] = seed;
-        b.ps_att[slot] = make_float4(att.x, att.y, att.z, at.w);
-        ++guided_n;
-      }
+    if (valid) {
+      if (PHYS) want = guided_pb_vertex(b, depth, i, o, p, nd, slot, guided_n);
+      else want = guided_compat_vertex(b, depth, i, o, p, nd, slot, guided_n);
     }
     const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want);
     if (want) {
       b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
       b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
     }
-  }
+  });
   warp_add32(&b.ctrl->guided_count, guided_n);
 }
 
@@ -816,8 +1067,9 @@ WaveBufs make_bufs(Renderer& r) {
   b.scenes = r.d_scenes;
   b.capacity = r.capacity;
   b.refill_busy_max = 32u - (r.opts.refill_idle ? std::min<uint32_t>(r.opts.refill_idle, 32u) : LISA_REFILL_IDLE);
-  b.guide_out = r.guide_out;
+  b.physical = r.opts.estimator == LISA_ESTIMATOR_PHYSICAL;
   b.train_rec = r.train_rec;
+  b.nee_light = r.nee_light;
   b.max_depth = r.max_depth;
   b.bsdf_fraction = r.opts.guide_bsdf_fraction;
   return b;
@@ -846,6 +1098,13 @@ struct StageTimer {
 };
 
 }  // namespace
+
+// Dynamic shared memory of the fused inference kernels.
+Status guided_infer_setup() {
+  LISA_CUDA(cudaFuncSetAttribute(k_guided_infer<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM));
+  LISA_CUDA(cudaFuncSetAttribute(k_guided_infer<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM));
+  return Status();
+}
 
 Status guide_collect(Renderer& r, int wave, int, cudaStream_t s) {
   WaveBufs b = make_bufs(r);
@@ -878,6 +1137,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
   const int acc_blocks = r.sm_count * 8;
   const bool counting = r.opts.count_traversal != 0;
   const bool guided = r.opts.mode == LISA_MODE_GUIDED;
+  const bool physical = r.opts.estimator == LISA_ESTIMATOR_PHYSICAL;
   for (size_t wv = 0; wv < waves.size(); ++wv) {
     const WaveDesc* wd = r.d_waves + wv;
     GuideSrc infer_src, train_src;
@@ -892,6 +1152,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       infer_src.ps_att = r.ps_att;
       infer_src.count = &r.ctrl->nee_count;
       infer_src.n = r.capacity;
+      infer_src.no_flag = physical ? 1u : 0u;
       for (int k = 0; k < 3; ++k) {
         infer_src.bmin[k] = sg.bvh.bmin[k];
         infer_src.bmax[k] = sg.bvh.bmax[k];
@@ -913,25 +1174,40 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         return Status();
       }));
       LISA_TRY(stage(1, [&] {
-        k_shade<<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d);
+        if (physical) k_shade<true><<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d);
+        else k_shade<false><<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d);
         return Status();
       }));
       LISA_TRY(stage(2, [&] {
-        if (guided) {
-          if (counting) k_nee<true, true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
-          else k_nee<false, true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+        const dim3 g(r.nee_blocks), t(r.nee_threads);
+        if (physical) {
+          if (guided) {
+            if (counting) k_nee_pb<true, true><<<g, t, 0, r.stream>>>(b, (int)d);
+            else k_nee_pb<false, true><<<g, t, 0, r.stream>>>(b, (int)d);
+          } else {
+            if (counting) k_nee_pb<true, false><<<g, t, 0, r.stream>>>(b, (int)d);
+            else k_nee_pb<false, false><<<g, t, 0, r.stream>>>(b, (int)d);
+          }
+        } else if (guided) {
+          if (counting) k_nee<true, true><<<g, t, 0, r.stream>>>(b, (int)d);
+          else k_nee<false, true><<<g, t, 0, r.stream>>>(b, (int)d);
         } else {
-          if (counting) k_nee<true><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
-          else k_nee<false><<<r.nee_blocks, r.nee_threads, 0, r.stream>>>(b, (int)d);
+          if (counting) k_nee<true><<<g, t, 0, r.stream>>>(b, (int)d);
+          else k_nee<false><<<g, t, 0, r.stream>>>(b, (int)d);
         }
         return Status();
       }));
       if (guided) {
-        LISA_TRY(stage(4, [&] { return guide_launch_infer(*net, infer_src, SRC_NEE, r.guide_out, r.capacity, r.stream); }));
         LISA_TRY(stage(4, [&] {
           WaveBufs bw = b;  // warm-up waves sample the BSDF only (c = 1)
           if (waves[wv].warm) bw.bsdf_fraction = 1.0f;
-          k_guided_bounce<<<r.shade_blocks, 256, 0, r.stream>>>(bw, (int)d);
+          const uint32_t grid = std::min<uint32_t>((r.capacity + 127) / 128, (uint32_t)(r.sm_count * INFER_BLOCKS_PER_SM));
+          if (physical)
+            k_guided_infer<true><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
+                                                                       bw, (int)d);
+          else
+            k_guided_infer<false><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
+                                                                        bw, (int)d);
           return Status();
         }));
       }
@@ -1265,7 +1541,7 @@ Status configure_launch(Renderer& r) {
   bps = std::min(bps, std::max(occ, 1));
   r.nee_threads = tthreads;
   r.nee_blocks = r.sm_count * bps;
-  LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade, 256, 0));
+  LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade<false>, 256, 0));
   r.shade_threads = 256;
   r.shade_blocks = r.sm_count * std::max(occ, 1);
   return Status();

@@ -21,9 +21,10 @@ struct WaveBufs {
   const SceneDev* scenes;
   uint32_t capacity;
   uint32_t refill_busy_max;  // persistent kernels refill a warp once at most this many lanes are busy
+  uint32_t physical;         // physically based estimator: ps_att.w = pdf of the last diffuse bounce
   // guided mode (null otherwise)
-  float* guide_out;   // per NEE entry: 40 network outputs -> mixture params
   float4* train_rec;  // per slot and depth: 5 float4 training record
+  float4* nee_light;  // guided physically based mode: per entry, the emitter sample (2 float4)
   uint32_t max_depth;
   float bsdf_fraction;  // one-sample MIS: probability of the BSDF strategy
 };

@@ -1,8 +1,8 @@
 """Image-quality studies: guided vs plain sampling at equal time, against a
 high-spp reference accumulated in FP64 on the GPU.
 
-  python -m lisa_gb300.study hard_indirect [--res 1024] [--spp 256] [--ref-spp 16384]
-  python -m lisa_gb300.study batch [--n 64] [--spp-scale 0.0625] [--ref-mult 16]
+  python -m lisa_gb300.study hard_indirect [--res 1024] [--spp 256] [--ref-spp 16384] [--estimator physical]
+  python -m lisa_gb300.study batch [--n 64] [--spp-scale 0.0625] [--ref-mult 16] [--estimator physical]
 
 relMSE = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2).
 Because the reference has finite spp, E[(x - ref)^2] = MSE(x) + Var(ref);
@@ -43,6 +43,10 @@ def _render(L, params, **opt):
     return r, st, wall
 
 
+def _estimator(L, args) -> int:
+    return L._native.LISA_ESTIMATOR_PHYSICAL if args.estimator == "physical" else L._native.LISA_ESTIMATOR_COMPAT
+
+
 def hard_indirect(args) -> List[dict]:
     import lisa_gb300 as L
 
@@ -51,7 +55,8 @@ def hard_indirect(args) -> List[dict]:
     out = []
     # reference: plain sampling, FP64 accumulation, progressive launches
     p_ref = L.params_from_scene(sc, num_samples=args.ref_spp)
-    ref = L.Renderer(p_ref, L.default_options(accum_fp64=1, seed=1000003))
+    est = _estimator(L, args)
+    ref = L.Renderer(p_ref, L.default_options(accum_fp64=1, seed=1000003, estimator=est))
     t0 = time.perf_counter()
     done = 0
     while done < args.ref_spp:
@@ -65,7 +70,7 @@ def hard_indirect(args) -> List[dict]:
     p = L.params_from_scene(sc)
     rows = {}
     for name, opt in (("plain", dict(seed=12)), ("guided", dict(seed=13, mode=L._native.LISA_MODE_GUIDED))):
-        r, st, wall = _render(L, p, **opt)
+        r, st, wall = _render(L, p, estimator=est, **opt)
         img = r.image()
         rows[name] = dict(ms=st.ms_device, wall_s=wall, rays=st.rays, relmse=relmse(img, R),
                           relmse_corrected=relmse(img, R, vom), guide_loss=st.guide_loss,
@@ -76,7 +81,8 @@ def hard_indirect(args) -> List[dict]:
     tp, tg = rows["plain"]["ms"], rows["guided"]["ms"]
     ep, eg = rows["plain"]["relmse_corrected"], rows["guided"]["relmse_corrected"]
     out.append({
-        "study": "hard_indirect", "scene": sc.name, "triangles": sc.num_triangles, "res": args.res,
+        "study": "hard_indirect", "estimator": args.estimator, "scene": sc.name, "triangles": sc.num_triangles,
+        "res": args.res,
         "spp": args.spp, "bounces": 8, "reference": {"spp": args.ref_spp, "accum": "fp64", "seconds": ref_s},
         "plain": rows["plain"], "guided": rows["guided"],
         "equal_time_relmse": {"plain": ep, "guided": eg * tg / tp},
@@ -92,11 +98,13 @@ def batch(args) -> List[dict]:
     scs = S.batch_scenes(n=args.n, seed=5, max_res=args.max_res)
     spp = [max(4, int(round(s.num_samples * args.spp_scale))) for s in scs]
     params = [L.params_from_scene(s, num_samples=k) for s, k in zip(scs, spp)]
-    tune_p = L.autotune(params, cache=args.cache)
-    tune_g = L.autotune(params, cache=args.cache, mode=G)
+    est = _estimator(L, args)
+    tune_p = L.autotune(params, cache=args.cache, estimator=est)
+    tune_g = L.autotune(params, cache=args.cache, mode=G, estimator=est)
     res = {}
     imgs = {}
-    for name, tune, opt in (("plain", tune_p, dict(seed=12)), ("guided", tune_g, dict(seed=13, mode=G))):
+    for name, tune, opt in (("plain", tune_p, dict(seed=12, estimator=est)),
+                            ("guided", tune_g, dict(seed=13, mode=G, estimator=est))):
         o = L.apply_tuning(tune, L.default_options(**opt))
         r = L.Renderer(params, o)
         r.render()  # warm-up: graph capture, guide training from scratch below
@@ -112,7 +120,7 @@ def batch(args) -> List[dict]:
     # per-scene reference: ref_mult x the spp, plain, FP64
     p_ref = [L.params_from_scene(s, num_samples=k * args.ref_mult) for s, k in zip(scs, spp)]
     t0 = time.perf_counter()
-    ref = L.Renderer(p_ref, L.apply_tuning(tune_p, L.default_options(accum_fp64=1, seed=1000003)))
+    ref = L.Renderer(p_ref, L.apply_tuning(tune_p, L.default_options(accum_fp64=1, seed=1000003, estimator=est)))
     ref.render()
     ref_s = time.perf_counter() - t0
     scenes_out = []
@@ -127,7 +135,7 @@ def batch(args) -> List[dict]:
                            "equal_time_guided": eg * tg / tp})
     ref.close()
     return [{
-        "study": "batch", "scenes": len(scs), "spp_scale": args.spp_scale,
+        "study": "batch", "estimator": args.estimator, "scenes": len(scs), "spp_scale": args.spp_scale,
         "total_paths": int(sum(s.width * s.height * k for s, k in zip(scs, spp))),
         "reference": {"spp_mult": args.ref_mult, "accum": "fp64", "seconds": ref_s},
         "plain": res["plain"], "guided": res["guided"], "per_scene": scenes_out,
@@ -140,7 +148,8 @@ def summary_md(rows: List[dict], cmd: str) -> str:
     lines = [f"Command: `{cmd}`", ""]
     for r in rows:
         if r["study"] == "hard_indirect":
-            lines += [f"## hard indirect ({r['scene']}, {r['triangles']:,} tris, {r['res']}^2, {r['spp']} spp)", "",
+            lines += [f"## hard indirect, {r['estimator']} estimator ({r['scene']}, {r['triangles']:,} tris, "
+                      f"{r['res']}^2, {r['spp']} spp)", "",
                       f"Reference: {r['reference']['spp']} spp plain, FP64 accumulation "
                       f"({r['reference']['seconds']:.0f} s).", "",
                       "| method | device ms | Mrays | relMSE | relMSE (ref. variance removed) |",
@@ -153,7 +162,8 @@ def summary_md(rows: List[dict], cmd: str) -> str:
                           f"{r['equal_time_relmse']['guided']:.6g}; guided time to plain's error = "
                           f"{r['time_to_plain_error']:.3f} x plain's time.", ""]
         else:
-            lines += [f"## batch of {r['scenes']} scenes (spp x {r['spp_scale']}, {r['total_paths']:,} paths)", "",
+            lines += [f"## batch of {r['scenes']} scenes, {r['estimator']} estimator (spp x {r['spp_scale']}, "
+                      f"{r['total_paths']:,} paths)", "",
                       "| method | device ms | Mrays/s | launches | tuning |", "|---|---|---|---|---|"]
             for m in ("plain", "guided"):
                 x = r[m]
@@ -189,6 +199,7 @@ def main(argv=None):
     b.add_argument("--cache", default=None, help="autotuner cache (JSON)")
     for p in (h, b):
         p.add_argument("--summary", default=None, help="write a markdown summary here")
+        p.add_argument("--estimator", default="compat", choices=["compat", "physical"])
     args = ap.parse_args(argv)
     rows = hard_indirect(args) if args.which == "hard_indirect" else batch(args)
     for r in rows:

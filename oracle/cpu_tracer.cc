@@ -20,6 +20,13 @@
 // file is compiled with -ffp-contract=off and no fast-math, and
 // pow(x,2)/pow(x,5) are written as products.
 //
+// It also restates the product's opt-in physically based estimator
+// (estimator = 1; no reference counterpart): emitter sampling by area x
+// luminance with two-sided emitters, cosine-weighted diffuse sampling,
+// power-heuristic MIS between the two, roughness as the weight of the
+// diffuse lobe against a mirror, and Schlick's Fresnel term evaluated on the
+// less dense side (the transmitted cosine when leaving a medium).
+//
 // Deliberate readings of the reference (shared with the product):
 //   * a zero direction (total internal reflection) is a miss, not traced;
 //   * occlusion queries return the closest hit (OptiX's terminate-on-first-
@@ -201,6 +208,18 @@ struct Bvh {
   std::vector<uint32_t> prims;
 };
 
+// Emitters of the physically based estimator: one 16-float record per
+// emissive triangle of positive area and luminance --
+// (v0.xyz, area pdf) (e1 = v1 - v0, material as int bits) (e2 = v2 - v0, 0)
+// (unit normal, 0) -- a CDF over area x luminance, and per material the
+// area pdf luminance / total of its triangles.
+struct Emitters {
+  std::vector<float> rec;
+  std::vector<float> cdf;
+  std::vector<float> mat_pdf;
+  uint32_t count = 0;
+};
+
 struct Ctx {
   const float* v = nullptr;   // 9 per triangle
   const float* n = nullptr;   // 9 per triangle
@@ -211,6 +230,7 @@ struct Ctx {
   float extent = 1.0f;
   Bvh bvh;
   bool use_bvh = false;
+  Emitters em;
 };
 
 void build_bvh(Ctx& c) {
@@ -417,6 +437,220 @@ V3 trace_path(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters& c
   return color;
 }
 
+// ---- physically based estimator (the product's opt-in mode) ----
+constexpr float PI_F = 3.14159265358979323846f;
+
+inline float luminance(float r, float g, float b) { return (0.2126f * r + 0.7152f * g) + 0.0722f * b; }
+
+// Emitter records, CDF and per-material area pdf, in triangle order.
+void build_emitters(Ctx& c) {
+  Emitters& e = c.em;
+  e.rec.clear();
+  e.cdf.clear();
+  e.count = 0;
+  const size_t M = c.cls.size();
+  e.mat_pdf.assign(M, 0.0f);
+  std::vector<float> lum(M, 0.0f);
+  for (size_t m = 0; m < M; ++m)
+    if (c.cls[m] == 2) lum[m] = luminance(c.emission[3 * m], c.emission[3 * m + 1], c.emission[3 * m + 2]);
+  std::vector<double> w;
+  for (uint32_t p = 0; p < c.T; ++p) {
+    const int m = c.mi[p];
+    if (c.cls[m] != 2 || !(lum[m] > 0.0f)) continue;
+    const float* t = c.v + 9ull * p;
+    const V3 v0 = v3(t[0], t[1], t[2]);
+    const V3 e1 = v3(t[3], t[4], t[5]) - v0, e2 = v3(t[6], t[7], t[8]) - v0;
+    const V3 cr = cross(e1, e2);
+    const float len = std::sqrt(dot(cr, cr));
+    const float area = 0.5f * len;
+    if (!(area > 0.0f)) continue;
+    const V3 n = cr * (1.0f / len);
+    int mbits;
+    std::memcpy(&mbits, &m, 4);
+    float mf;
+    std::memcpy(&mf, &mbits, 4);
+    const float r[16] = {v0.x, v0.y, v0.z, 0.0f, e1.x, e1.y, e1.z, mf, e2.x, e2.y, e2.z, 0.0f, n.x, n.y, n.z, 0.0f};
+    e.rec.insert(e.rec.end(), r, r + 16);
+    w.push_back((double)area * (double)lum[m]);
+  }
+  e.count = (uint32_t)w.size();
+  if (!e.count) return;
+  double total = 0.0;
+  for (double x : w) total += x;
+  double acc = 0.0;
+  e.cdf.resize(e.count);
+  for (uint32_t i = 0; i < e.count; ++i) {
+    acc += w[i];
+    e.cdf[i] = (float)(acc / total);
+  }
+  e.cdf[e.count - 1] = 1.0f;
+  for (size_t m = 0; m < M; ++m) e.mat_pdf[m] = (float)((double)lum[m] / total);
+  for (uint32_t i = 0; i < e.count; ++i) {
+    int m;
+    std::memcpy(&m, &e.rec[16ull * i + 7], 4);
+    e.rec[16ull * i + 3] = e.mat_pdf[m];
+  }
+}
+
+// unit geometric normal of triangle p (cross(v1 - v0, v2 - v0) normalised)
+V3 tri_normal(const Ctx& c, int p) {
+  const float* t = c.v + 9ull * p;
+  const V3 v0 = v3(t[0], t[1], t[2]);
+  const V3 cr = cross(v3(t[3], t[4], t[5]) - v0, v3(t[6], t[7], t[8]) - v0);
+  return cr * (1.0f / std::sqrt(dot(cr, cr)));
+}
+
+// Orthonormal basis around a unit vector (Duff et al., JCGT 2017).
+void onb(V3 n, V3& t, V3& b) {
+  const float sign = std::copysign(1.0f, n.z);
+  const float a = -1.0f / (sign + n.z);
+  const float bb = (n.x * n.y) * a;
+  t = v3(1.0f + ((sign * n.x) * n.x) * a, sign * bb, -(sign * n.x));
+  b = v3(bb, sign + (n.y * n.y) * a, -n.y);
+}
+
+// Cosine-weighted direction about n: a uniform point of the unit disk by
+// rejection (at most 16 pairs, then the centre), lifted to the hemisphere
+// (Malley's method).
+V3 cosine_dir(V3 n, uint32_t& seed) {
+  float x = 0.0f, y = 0.0f, r2 = 0.0f;
+  for (int k = 0; k < 16; ++k) {
+    x = rng11(seed);
+    y = rng11(seed);
+    r2 = x * x + y * y;
+    if (r2 < 1.0f) break;
+  }
+  if (!(r2 < 1.0f)) x = y = r2 = 0.0f;
+  const float z = std::sqrt(std::fmax(0.0f, 1.0f - r2));
+  V3 t, b;
+  onb(n, t, b);
+  return normalize((x * t + y * b) + z * n);
+}
+
+// A point of an emitter, chosen by area x luminance, uniform on it.
+// Returns the record index.
+uint32_t sample_emitter(const Emitters& e, uint32_t& seed, V3& y) {
+  const float u0 = rnd(seed), u1 = rnd(seed), u2 = rnd(seed);
+  uint32_t lo = 0, hi = e.count - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (u0 < e.cdf[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  const float* r = e.rec.data() + 16ull * lo;
+  const float a = std::sqrt(u1);
+  const float bu = a * (1.0f - u2), bv = a * u2;
+  y = v3(r[0], r[1], r[2]) + (bu * v3(r[4], r[5], r[6]) + bv * v3(r[8], r[9], r[10]));
+  return lo;
+}
+
+// One path of the physically based estimator.
+V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters& cnt) {
+  V3 color = v3(0.0f, 0.0f, 0.0f), att = v3(1.0f, 1.0f, 1.0f);
+  float prev_pdf = 0.0f;  // solid-angle pdf of the last diffuse bounce; 0 after camera / specular
+  const Emitters& em = c.em;
+  for (int i = 0; i < bounces; ++i) {
+    if (is_zero(d)) break;
+    if (i == 0) ++cnt.primary; else ++cnt.bounce;
+    int prim;
+    float t;
+    closest(c, o, d, 1e-4f, 1e16f, &prim, &t);
+    if (prim < 0) break;
+    const int m = c.mi[prim];
+    const V3 le = v3(c.emission[3 * m], c.emission[3 * m + 1], c.emission[3 * m + 2]);
+    if (c.cls[m] == 2) {
+      if (prev_pdf > 0.0f) {
+        const float cos_y = std::fabs(dot(tri_normal(c, prim), d));
+        float w = 0.0f;
+        if (cos_y > 0.0f) {
+          const float pl = (em.mat_pdf[m] * (t * t)) / cos_y;
+          w = (prev_pdf * prev_pdf) / ((prev_pdf * prev_pdf) + (pl * pl));
+        }
+        color = color + (le * att) * w;
+      } else {
+        color = color + le * att;
+      }
+      break;
+    }
+    const V3 p = o + t * d;
+    const float* tv = c.v + 9ull * prim;
+    const float* tn = c.n + 9ull * prim;
+    const V3 N = barycentric_normal(p, v3(tn[0], tn[1], tn[2]), v3(tn[3], tn[4], tn[5]), v3(tn[6], tn[7], tn[8]),
+                                    v3(tv[0], tv[1], tv[2]), v3(tv[3], tv[4], tv[5]), v3(tv[6], tv[7], tv[8]));
+    const V3 albedo = v3(c.albedo[3 * m], c.albedo[3 * m + 1], c.albedo[3 * m + 2]);
+    if (c.cls[m] == 1) {
+      float cosI = dot(d, N);
+      float eta;
+      V3 nrm;
+      if (cosI < 0.0f) {
+        cosI = -cosI;
+        eta = 1.0f / c.ior[m];
+        nrm = N;
+      } else {
+        att = att * albedo;
+        eta = c.ior[m];
+        nrm = -N;
+      }
+      V3 nd;
+      if (eta == 1.0f) {
+        nd = d;
+      } else {
+        const float cost2 = 1.0f - (eta * eta) * (1.0f - cosI * cosI);
+        if (cost2 <= 0.0f) {
+          nd = reflect(d, nrm);  // total internal reflection
+        } else {
+          const float F = fresnel(eta > 1.0f ? std::sqrt(cost2) : cosI, eta);
+          if (rnd(seed) <= F) nd = reflect(d, nrm);
+          else nd = refract(cosI, d, nrm, eta);
+        }
+      }
+      prev_pdf = 0.0f;
+      d = nd;
+      o = p;
+      continue;
+    }
+    att = att * albedo;
+    const V3 Ns = dot(N, d) < 0.0f ? N : -N;
+    const float r = c.rough[m];
+    if (r > 0.0f && em.count > 0) {
+      V3 y;
+      const uint32_t k = sample_emitter(em, seed, y);
+      const float* rec = em.rec.data() + 16ull * k;
+      const V3 w = y - p;
+      const float d2 = dot(w, w);
+      const float dist = std::sqrt(d2);
+      const V3 wi = w * (1.0f / dist);
+      const float cos_x = dot(Ns, wi);
+      const float cos_y = std::fabs(dot(v3(rec[12], rec[13], rec[14]), wi));
+      if (cos_x > 0.0f && cos_y > 0.0f && dist > 0.0f) {
+        ++cnt.shadow;
+        int hp;
+        float ht;
+        closest(c, p, wi, 1e-4f, dist * (1.0f - 0.0009765625f), &hp, &ht);
+        if (hp < 0) {
+          int em_m;
+          std::memcpy(&em_m, &rec[7], 4);
+          const V3 le_y = v3(c.emission[3 * em_m], c.emission[3 * em_m + 1], c.emission[3 * em_m + 2]);
+          const float pl = (rec[3] * d2) / cos_y;
+          const float fcos = r * (cos_x / PI_F);
+          const float wl = (pl * pl) / ((pl * pl) + (fcos * fcos));
+          color = color + ((att * le_y) * (fcos / pl)) * wl;
+        }
+      }
+    }
+    const bool diffuse = r >= 1.0f || (r > 0.0f && rnd(seed) < r);
+    if (diffuse) {
+      d = cosine_dir(Ns, seed);
+      prev_pdf = r * (dot(Ns, d) / PI_F);
+    } else {
+      d = reflect(d, Ns);
+      prev_pdf = 0.0f;
+    }
+    o = p;
+  }
+  return color;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -444,6 +678,7 @@ struct oracle_scene {
   uint32_t seed;
   uint64_t sample_base;
   uint32_t subframe;
+  uint32_t estimator;  // 0 = the reference estimator, 1 = physically based
 };
 
 static void make_ctx(const oracle_scene* s, int use_bvh, Ctx& c) {
@@ -478,6 +713,7 @@ static void make_ctx(const oracle_scene* s, int use_bvh, Ctx& c) {
   c.extent = e2 > 0 ? (float)std::sqrt(e2) : 1.0f;
   c.use_bvh = use_bvh != 0;
   if (c.use_bvh) build_bvh(c);
+  if (c.mi) build_emitters(c);
 }
 
 // Closest hit of n rays (8 floats each: ox oy oz tmin dx dy dz tmax).
@@ -546,7 +782,8 @@ int oracle_ctx_render(void* ctx, const oracle_scene* s, int threads, uint32_t px
       const float dx = (2.0f * (float)x + jx) / fw - 1.0f;
       const float dy = (2.0f * (float)y + jy) / fh - 1.0f;
       const V3 dir = normalize((dx * U + dy * V) + W);
-      const V3 col = trace_path(c, eye, dir, (int)s->bounces, seed, cnt);
+      const V3 col = s->estimator == 1 ? trace_path_pb(c, eye, dir, (int)s->bounces, seed, cnt)
+                                       : trace_path(c, eye, dir, (int)s->bounces, seed, cnt);
       const float cc[3] = {col.x, col.y, col.z};
       for (int k = 0; k < 3; ++k) {
         a[k] += cc[k];

@@ -21,7 +21,7 @@ def test_reference_variance_correction_is_unbiased():
 
 
 def test_summary_renders():
-    row = {"study": "hard_indirect", "scene": "s", "triangles": 10, "res": 8, "spp": 4,
+    row = {"study": "hard_indirect", "estimator": "compat", "scene": "s", "triangles": 10, "res": 8, "spp": 4,
            "reference": {"spp": 64, "seconds": 1.0},
            "plain": {"ms": 1.0, "rays": 1e6, "relmse": 0.2, "relmse_corrected": 0.1},
            "guided": {"ms": 1.1, "rays": 1e6, "relmse": 0.1, "relmse_corrected": 0.05},
