@@ -121,15 +121,26 @@ typedef struct lisa_options {
                                 kernels (node visits / triangle tests)        */
   uint32_t guide_warmup_waves;/* first waves train the guide but sample the
                                 BSDF only                                      */
-  uint32_t guide_steps_per_wave;/* Adam steps per wave, each on its own slice
-                                of guide_train_batch samples (0 = 1)           */
+  uint32_t guide_steps_per_wave;/* Adam steps after a guided wave per 4 Mi of
+                                its paths (at least one), each on its own slice
+                                of guide_train_batch samples                  */
   uint32_t guide_spp_per_wave;/* guided mode: at most this many samples per
-                                pixel per wave, so every scene trains over
-                                several waves (0 = fill the wavefront)         */
+                                pixel per wave (more for images under 1 Mi
+                                pixels), so every scene trains over several
+                                waves (0 = fill the wavefront)                */
   uint32_t refill_idle;      /* persistent traversal kernels take new work once
                                 this many of a warp's 32 lanes are idle
                                 (1..32; 0 = 12)                               */
   uint32_t estimator;        /* LISA_ESTIMATOR_*                               */
+  uint32_t bvh_lbvh_only;    /* 1 = keep the plain LBVH: skip its SAH treelet
+                                restructuring before the 8-wide collapse      */
+  uint32_t guide_min_spp;    /* guided mode guides the scenes with at least
+                                this many samples per pixel (num_samples);
+                                the others render plain, packed together     */
+  uint32_t guide_max_depth;  /* the guide draws the bounces of the first this
+                                many vertices of a path; deeper ones sample
+                                the BSDF (0 = every vertex)                  */
+  uint32_t reserved;
 } lisa_options;
 
 /* Per-call statistics.  Ray counts are rays actually traced: primary +

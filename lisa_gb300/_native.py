@@ -68,7 +68,8 @@ class Options(C.Structure):
                 ("alloc_cap_bytes", C.c_uint64), ("count_traversal", C.c_uint32),
                 ("guide_warmup_waves", C.c_uint32), ("guide_steps_per_wave", C.c_uint32),
                 ("guide_spp_per_wave", C.c_uint32), ("refill_idle", C.c_uint32),
-                ("estimator", C.c_uint32)]
+                ("estimator", C.c_uint32), ("bvh_lbvh_only", C.c_uint32), ("guide_min_spp", C.c_uint32),
+                ("guide_max_depth", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class RenderStats(C.Structure):

@@ -267,7 +267,7 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   Status st;
   {
     TempDeviceBufs tmp;
-    st = build_bvh(d_v, T, r.stream, tmp, r.arena, &s.nodes, &s.tris, &s.bvh, d_m);
+    st = build_bvh(d_v, T, r.stream, tmp, r.arena, &s.nodes, &s.tris, &s.bvh, d_m, r.opts.bvh_lbvh_only == 0);
     cudaStreamSynchronize(r.stream);
   }
   if (d_v) cudaFree(d_v);
@@ -527,13 +527,14 @@ void lisa_options_default(lisa_options* o) {
   o->rng = LISA_RNG_PER_SAMPLE;
   o->use_graph = 1;
   o->guide_bsdf_fraction = 0.5f;
-  // 32 Adam steps of 16384 samples per wave at lr 1e-3, after 4 warm-up
-  // waves, with at most 16 spp per wave
+  // 64 Adam steps of 16384 samples per 4 Mi paths at lr 1e-3, after 4
+  // warm-up waves, with at most 16 spp per wave
   o->guide_lr = 1e-3f;
   o->guide_train_batch = 16384;
   o->guide_warmup_waves = 4;
-  o->guide_steps_per_wave = 32;
+  o->guide_steps_per_wave = 64;
   o->guide_spp_per_wave = 16;
+  o->guide_min_spp = 64;
 }
 
 int lisa_renderer_create(const lisa_renderer_params* params, const lisa_options* opts, lisa_renderer** out) {

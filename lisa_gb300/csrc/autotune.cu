@@ -232,9 +232,9 @@ std::string tuning_key(const cudaDeviceProp& p, const lisa_renderer_params* sc, 
   for (char& c : name)
     if (!std::isalnum((unsigned char)c)) c = '_';
   char buf[160];
-  std::snprintf(buf, sizeof(buf), "%s|sm%d|cc%d.%d|mode%u|rng%u|px2^%u|tri2^%u|b%u|n2^%u", name.c_str(),
-                p.multiProcessorCount, p.major, p.minor, o.mode, o.rng, log2_bucket(px), log2_bucket(tris), bounces,
-                log2_bucket((uint64_t)n));
+  std::snprintf(buf, sizeof(buf), "%s|sm%d|cc%d.%d|mode%u|est%u|rng%u|px2^%u|tri2^%u|b%u|n2^%u", name.c_str(),
+                p.multiProcessorCount, p.major, p.minor, o.mode, o.estimator, o.rng, log2_bucket(px),
+                log2_bucket(tris), bounces, log2_bucket((uint64_t)n));
   return buf;
 }
 

@@ -353,6 +353,192 @@ __global__ void k_bottom_up(uint32_t n, const uint32_t* __restrict__ vals, const
   }
 }
 
+// ---- SAH refinement: treelet restructuring -----------------------------------
+//
+// One bottom-up pass over the binary LBVH (Karras & Aila, "Fast Parallel
+// Construction of High-Quality Bounding Volume Hierarchies", HPG 2013): the
+// thread that completes a node computes its box, primitive count and SAH
+// cost, then takes the treelet of up to 7 leaves under it (grown by opening
+// the treelet leaf of largest area) and rebuilds the treelet's internal
+// nodes in the topology of least SAH cost, found by dynamic programming over
+// the leaf subsets.  The treelet's leaves and everything below them stay as
+// they are; every node keeps a box equal to the union of its children's.
+// Node counts and costs overwrite the Karras ranges (first -> count,
+// last -> cost bits), which the collapse no longer needs.
+
+constexpr float SAH_CI = 1.2f;  // cost of a node visit relative to a triangle test
+constexpr float SAH_CT = 1.0f;
+constexpr int TL = 7;           // treelet leaves
+constexpr uint32_t TREELET_MIN_PRIMS = 16;  // smaller subtrees keep their LBVH topology (the 8-wide collapse flattens them)
+
+__device__ __forceinline__ float4 box_min(float4 a, float4 b) {
+  return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
+}
+__device__ __forceinline__ float4 box_max(float4 a, float4 b) {
+  return make_float4(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), 0.0f);
+}
+__device__ __forceinline__ float box_half_area(float4 lo, float4 hi) {
+  const float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
+  return x * y + y * z + z * x;
+}
+
+struct SahTree {
+  uint32_t n;
+  const uint32_t* vals;
+  const float4* plo;
+  const float4* phi;
+  uint32_t* parent_leaf;
+  uint32_t* parent_int;
+  uint32_t* left;
+  uint32_t* right;
+  float4* ilo;
+  float4* ihi;
+  uint32_t* count;  // per internal node: primitives below
+  float* cost;      // per internal node: SAH cost of its subtree
+  uint32_t* flags;
+};
+
+// box, count and cost of a child (leaf or internal node, already complete)
+__device__ __forceinline__ void sah_child(const SahTree& t, uint32_t c, float4& lo, float4& hi, uint32_t& cnt,
+                                          float& cost) {
+  if (c & LEAF_BIT) {
+    const uint32_t q = t.vals[c & ~LEAF_BIT];
+    lo = t.plo[q];
+    hi = t.phi[q];
+    cnt = 1;
+    cost = SAH_CT * box_half_area(lo, hi);
+  } else {
+    lo = __ldcg(t.ilo + c);
+    hi = __ldcg(t.ihi + c);
+    cnt = __ldcg(t.count + c);
+    cost = __ldcg(t.cost + c);
+  }
+}
+
+__device__ void treelet_optimize(const SahTree& t, uint32_t root) {
+  uint32_t leaf[TL], inner[TL - 2];
+  float4 llo[TL], lhi[TL];
+  float lcost[TL];
+  uint32_t lcnt[TL];
+  int nl = 2, ni = 0;
+  leaf[0] = __ldcg(t.left + root);
+  leaf[1] = __ldcg(t.right + root);
+  sah_child(t, leaf[0], llo[0], lhi[0], lcnt[0], lcost[0]);
+  sah_child(t, leaf[1], llo[1], lhi[1], lcnt[1], lcost[1]);
+  while (nl < TL) {
+    int best = -1;
+    float ba = -1.0f;
+    for (int k = 0; k < nl; ++k) {
+      if (leaf[k] & LEAF_BIT) continue;
+      const float a = box_half_area(llo[k], lhi[k]);
+      if (a > ba) {
+        ba = a;
+        best = k;
+      }
+    }
+    if (best < 0) break;
+    const uint32_t c = leaf[best];
+    inner[ni++] = c;
+    leaf[best] = __ldcg(t.left + c);
+    leaf[nl] = __ldcg(t.right + c);
+    sah_child(t, leaf[best], llo[best], lhi[best], lcnt[best], lcost[best]);
+    sah_child(t, leaf[nl], llo[nl], lhi[nl], lcnt[nl], lcost[nl]);
+    ++nl;
+  }
+  if (nl < 3) return;  // two leaves have one topology
+  const uint32_t full = (1u << nl) - 1u;
+  float opt[1 << TL];
+  uint8_t split[1 << TL];
+  for (uint32_t sset = 1; sset <= full; ++sset) {
+    if ((sset & (sset - 1u)) == 0u) {
+      opt[sset] = lcost[__ffs(sset) - 1];
+      split[sset] = 0;
+      continue;
+    }
+    float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+    for (int k = 0; k < nl; ++k)
+      if (sset & (1u << k)) {
+        lo = box_min(lo, llo[k]);
+        hi = box_max(hi, lhi[k]);
+      }
+    const uint32_t low = sset & (0u - sset), rest = sset ^ low;
+    float best = opt[low] + opt[rest];
+    uint32_t bp = low;
+    // partitions (P, S \ P) with the lowest member in P, each once:
+    // P = low + a nonempty proper subset of the rest
+    for (uint32_t q = (rest - 1u) & rest; q; q = (q - 1u) & rest) {
+      const uint32_t pset = q | low;
+      const float c = opt[pset] + opt[sset ^ pset];
+      if (c < best) {
+        best = c;
+        bp = pset;
+      }
+    }
+    opt[sset] = SAH_CI * box_half_area(lo, hi) + best;
+    split[sset] = (uint8_t)bp;
+  }
+  if (!(opt[full] < __ldcg(t.cost + root) * (1.0f - 1e-6f))) return;  // the present topology is as good
+  // rebuild: the root keeps its id, the other internal subsets reuse inner[]
+  uint32_t st_set[TL], st_node[TL];
+  int sp = 0, next = 0;
+  st_set[sp] = full;
+  st_node[sp++] = root;
+  while (sp) {
+    --sp;
+    const uint32_t sset = st_set[sp], node = st_node[sp];
+    const uint32_t part[2] = {split[sset], sset ^ (uint32_t)split[sset]};
+    uint32_t ch[2];
+    for (int h = 0; h < 2; ++h) {
+      if ((part[h] & (part[h] - 1u)) == 0u) {
+        ch[h] = leaf[__ffs(part[h]) - 1];
+      } else {
+        ch[h] = inner[next++];
+        st_set[sp] = part[h];
+        st_node[sp++] = ch[h];
+      }
+      if (ch[h] & LEAF_BIT) __stcg(t.parent_leaf + (ch[h] & ~LEAF_BIT), node);
+      else __stcg(t.parent_int + ch[h], node);
+    }
+    __stcg(t.left + node, ch[0]);
+    __stcg(t.right + node, ch[1]);
+    float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+    uint32_t cnt = 0;
+    for (int k = 0; k < nl; ++k)
+      if (sset & (1u << k)) {
+        lo = box_min(lo, llo[k]);
+        hi = box_max(hi, lhi[k]);
+        cnt += lcnt[k];
+      }
+    __stcg(t.ilo + node, lo);
+    __stcg(t.ihi + node, hi);
+    __stcg(t.count + node, cnt);
+    __stcg(t.cost + node, opt[sset]);
+  }
+}
+
+__global__ void k_bottom_up_sah(SahTree t, int refine) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.n || t.n < 2) return;
+  uint32_t p = t.parent_leaf[i];
+  while (p != 0xffffffffu) {
+    __threadfence();
+    if (atomicAdd(&t.flags[p], 1u) == 0u) return;
+    __threadfence();
+    float4 a0, a1, b0, b1;
+    uint32_t ca, cb;
+    float sa, sb;
+    sah_child(t, __ldcg(t.left + p), a0, a1, ca, sa);
+    sah_child(t, __ldcg(t.right + p), b0, b1, cb, sb);
+    const float4 lo = box_min(a0, b0), hi = box_max(a1, b1);
+    __stcg(t.ilo + p, lo);
+    __stcg(t.ihi + p, hi);
+    __stcg(t.count + p, ca + cb);
+    __stcg(t.cost + p, SAH_CI * box_half_area(lo, hi) + sa + sb);
+    if (refine && ca + cb >= TREELET_MIN_PRIMS) treelet_optimize(t, p);
+    p = __ldcg(t.parent_int + p);
+  }
+}
+
 // ---- collapse to 8-wide compressed nodes -------------------------------------
 struct CollapseArgs {
   uint32_t n;
@@ -363,8 +549,7 @@ struct CollapseArgs {
   const float4* ihi;
   const uint32_t* left;
   const uint32_t* right;
-  const uint32_t* first;
-  const uint32_t* last;
+  const uint32_t* count;  // primitives below each internal node
   const float* verts;
   const int32_t* mats;  // material per triangle, or null
   uint4* nodes;
@@ -373,10 +558,7 @@ struct CollapseArgs {
 };
 
 __device__ __forceinline__ uint32_t sub_count(const CollapseArgs& a, uint32_t c) {
-  return (c & LEAF_BIT) ? 1u : (a.last[c] - a.first[c] + 1u);
-}
-__device__ __forceinline__ uint32_t sub_first(const CollapseArgs& a, uint32_t c) {
-  return (c & LEAF_BIT) ? (c & ~LEAF_BIT) : a.first[c];
+  return (c & LEAF_BIT) ? 1u : a.count[c];
 }
 __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
   const float x = hi.x - lo.x, y = hi.y - lo.y, z = hi.z - lo.z;
@@ -481,9 +663,21 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ work, uint3
       ++rank;
     } else {
       meta[k] = (uint8_t)((cnt << 5) | toff);
-      const uint32_t f0 = sub_first(a, cand[k]);
+      // the (at most 3) primitives below, left to right
+      uint32_t leaves[3], st[4];
+      int nlv = 0, sp = 0;
+      st[sp++] = cand[k];
+      while (sp) {
+        const uint32_t c = st[--sp];
+        if (c & LEAF_BIT) {
+          leaves[nlv++] = c & ~LEAF_BIT;
+        } else {
+          st[sp++] = a.right[c];
+          st[sp++] = a.left[c];
+        }
+      }
       for (uint32_t q = 0; q < cnt; ++q) {
-        const uint32_t prim = a.vals[f0 + q];
+        const uint32_t prim = a.vals[leaves[q]];
         const float* t = a.verts + 9ull * prim;
         float4* o = a.tris + 3ull * (tri_base + toff + q);
         o[0] = make_float4(t[0], t[1], t[2], __int_as_float((int)prim));
@@ -565,7 +759,7 @@ size_t bvh_temp_bytes(uint32_t n) {
 size_t bvh_output_bytes(uint32_t n) { return (size_t)(al256(80ull * (n + 1)) + al256(48ull * n)); }
 
 Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource& tmp, ScratchSource& out,
-                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info, const int32_t* d_mat) {
+                 uint4** d_nodes, float4** d_tris, BvhBuildResult* info, const int32_t* d_mat, bool refine) {
   auto t0 = std::chrono::steady_clock::now();
   if (n == 0) {
     *d_nodes = nullptr;
@@ -621,7 +815,10 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource
   if (n > 1) {
     k_karras<<<cdiv(n - 1, 256), 256, 0, s>>>(keys, n, left, right, first, last, par_int, par_leaf);
     LISA_CUDA(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * n, s));
-    k_bottom_up<<<cdiv(n, 256), 256, 0, s>>>(n, vals, plo, phi, par_leaf, par_int, left, right, ilo, ihi, flags);
+    // boxes, counts and SAH costs bottom up, with treelet restructuring
+    // unless refine is off; first/last become count/cost
+    const SahTree st{n, vals, plo, phi, par_leaf, par_int, left, right, ilo, ihi, first, (float*)last, flags};
+    k_bottom_up_sah<<<cdiv(n, 256), 256, 0, s>>>(st, refine ? 1 : 0);
     LISA_CUDA(cudaGetLastError());
   }
   // outputs
@@ -633,7 +830,7 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource
   LISA_CUDA(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
   const uint2 root = make_uint2(0u, n > 1 ? 0u : LEAF_BIT);
   LISA_CUDA(cudaMemcpyAsync(work0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
-  CollapseArgs a{n, vals, plo, phi, ilo, ihi, left, right, first, last, d_verts, d_mat, nodes, tris, counters};
+  CollapseArgs a{n, vals, plo, phi, ilo, ihi, left, right, first, d_verts, d_mat, nodes, tris, counters};
   uint32_t nwork = 1, depth = 0;
   uint2 *wi = work0, *wo = work1;
   while (nwork > 0) {

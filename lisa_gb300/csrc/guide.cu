@@ -420,8 +420,8 @@ static int sm_count_current() {
 }
 
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n, cudaStream_t s) {
-  const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
-  const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current() * INFER_BLOCKS_PER_SM);
+  const uint32_t pairs = std::max<uint32_t>(1, (max_n + 255) / 256);  // two tiles of 128 per CTA
+  const uint32_t grid = std::min<uint32_t>(pairs, (uint32_t)sm_count_current() * INFER_BLOCKS_PER_SM);
   if (src_kind == SRC_RAW)
     k_guide_infer<SRC_RAW><<<grid, 128, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
   else
@@ -477,7 +477,10 @@ Status guide_renderer_init(Renderer& r) {
   r.max_depth = maxd;
   const uint32_t chunk = std::max<uint32_t>(128, (r.opts.guide_train_batch + 127) / 128 * 128);
   r.guide_chunk = chunk;
-  const uint32_t B = chunk * std::max<uint32_t>(1, r.opts.guide_steps_per_wave);
+  // Adam steps of a wave: guide_steps_per_wave per 4 Mi paths, at least one
+  r.guide_max_steps = std::max<uint32_t>(
+      1u, (uint32_t)(((uint64_t)r.capacity * r.opts.guide_steps_per_wave + (1ull << 22) - 1) >> 22));
+  const uint32_t B = chunk * r.guide_max_steps;
   r.guide_batch_cap = B;
   if (!(r.opts.guide_bsdf_fraction >= 0.0f && r.opts.guide_bsdf_fraction <= 1.0f))
     return Status::invalid("guide_bsdf_fraction must be in [0, 1]");

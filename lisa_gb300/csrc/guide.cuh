@@ -52,7 +52,7 @@ struct GuideSrc {
 Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s);
 // Fills n training samples from the wave's guided-vertex records (host
 // launcher in wavefront.cu).
-Status guide_collect(Renderer& r, int wave, int scene, cudaStream_t s);
+Status guide_collect(Renderer& r, int wave, uint32_t cap, cudaStream_t s);
 // outputs: max_n x 40 floats (entries beyond the live count are not written)
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n,
                           cudaStream_t s);

@@ -119,8 +119,8 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
 
 // + 1024 for the manual 1024-byte alignment, + 2 KB of slack after the last
 // operand tile.  Three CTAs share an SM (3 x 75.8 KB of shared memory,
-// 3 x 64 TMEM columns, <= 168 registers a thread), so one CTA's tensor-core
-// waits and TMEM round trips overlap the others' epilogues.
+// 3 x 128 TMEM columns, <= 168 registers a thread), each with two tiles in
+// flight.
 constexpr int INFER_SMEM = FWD_BYTES + 2 * 16384 + 1024 + 2048;
 constexpr int INFER_BLOCKS_PER_SM = 3;
 
@@ -129,6 +129,11 @@ constexpr int INFER_BLOCKS_PER_SM = 3;
 // i < n; o = the 40 outputs, bias included).  All 128 threads call epi
 // together, so it may use warp-collective operations.  Needs INFER_SMEM
 // bytes of dynamic shared memory and 128 threads.
+//
+// Two tiles are in flight per CTA: while the threads run the epilogue of one
+// tile's layer (TMEM -> bias, ReLU -> BF16 rows), the tensor core runs the
+// other tile's layer.  A layer's output overwrites its input tile in shared
+// memory: the MMA that read it has completed when the epilogue starts.
 template <int SRC, class Epi>
 __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, const float* __restrict__ master,
                                             const GuideSrc& src, uint32_t* status, Epi&& epi) {
@@ -136,7 +141,7 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
   uint8_t* act[2] = {smem + FWD_BYTES, smem + FWD_BYTES + 16384};
-  __shared__ uint64_t mbar;
+  __shared__ uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   __shared__ __align__(16) float s_bias[4 * 64 + 48];
@@ -144,12 +149,13 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   // samples [src.first, n)
   const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
   const uint32_t ntiles = (n - src.first + 127) / 128;
-  if (blockIdx.x >= ntiles) return;
+  if (2 * blockIdx.x >= ntiles) return;
   if (tid == 0) {
-    tc::mbar_init(&mbar, 1);
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
     failed = 0;
   }
-  if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
   for (int c = tid; c < FWD_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
   for (int k = tid; k < 4 * 64 + 48; k += 128) s_bias[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
   tc::fence_smem_async();
@@ -157,64 +163,96 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
-  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-  uint32_t phase = 0;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint32_t i = src.first + t * 128 + tid;
-    {
-      float f[64];
-      if (i < n) load_features<SRC>(src, i, f);
-      else
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  // thread 0's view of the two barriers: parity of the next completion, and
+  // whether a committed MMA has not been waited for
+  uint32_t phase[2] = {0, 0};
+  bool busy[2] = {false, false};
+  auto weights = [&](int l) { return w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128; };
+  auto issue = [&](int k, int l) {
+    issue_layer(tmem + 64u * k, act[k], weights(l), l < 4 ? 64u : 48u, &mbar[k]);
+    busy[k] = true;
+  };
+  for (uint32_t t0 = 2 * blockIdx.x; t0 < ntiles && !failed; t0 += 2 * gridDim.x) {
+    const int nt = t0 + 1 < ntiles ? 2 : 1;  // tiles of this pair (uniform over the block)
+    uint32_t idx[2];
 #pragma unroll
-        for (int k = 0; k < 64; ++k) f[k] = 0.0f;
-      store_row_bf16(act[0], tid, f);
+    for (int k = 0; k < 2; ++k) {
+      idx[k] = src.first + (t0 + k) * 128 + tid;
+      if (k < nt) {
+        float f[64];
+        if (idx[k] < n) load_features<SRC>(src, idx[k], f);
+        else
+#pragma unroll
+          for (int q = 0; q < 64; ++q) f[q] = 0.0f;
+        store_row_bf16(act[k], tid, f);
+      }
     }
-    int cur = 0;
+    tc::fence_smem_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0)
+      for (int k = 0; k < nt; ++k) issue(k, 0);
 #pragma unroll 1
     for (int l = 0; l < 5; ++l) {
-      tc::fence_smem_async();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      if (tid == 0) {
-        issue_layer(tmem, act[cur], w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, l < 4 ? 64u : 48u, &mbar);
-        if (!tc::mbar_wait(&mbar, phase)) {
-          atomicOr(status, ST_GUIDE_NONFINITE << 1);
-          failed = 1;
+#pragma unroll 1
+      for (int k = 0; k < nt; ++k) {
+        if (tid == 0) {
+          if (tc::mbar_wait(&mbar[k], phase[k])) {
+            phase[k] ^= 1;
+            busy[k] = false;
+          } else {
+            atomicOr(status, ST_GUIDE_NONFINITE << 1);
+            failed = 1;
+          }
+        }
+        __syncthreads();  // the others learn of the finished MMA here
+        tc::fence_after_sync();
+        if (failed) break;
+        const uint32_t lane_addr = tmem + 64u * k + lane_off;
+        float acc[64];
+        if (l < 4) {
+          tc::tmem_ld16x<4>(lane_addr, acc);
+          const float4* bb = reinterpret_cast<const float4*>(s_bias + 64 * l);
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const float4 b4 = bb[q];
+            acc[4 * q] = fmaxf(acc[4 * q] + b4.x, 0.0f);
+            acc[4 * q + 1] = fmaxf(acc[4 * q + 1] + b4.y, 0.0f);
+            acc[4 * q + 2] = fmaxf(acc[4 * q + 2] + b4.z, 0.0f);
+            acc[4 * q + 3] = fmaxf(acc[4 * q + 3] + b4.w, 0.0f);
+          }
+          store_row_bf16(act[k], tid, acc);  // H_l over H_{l-1}
+          tc::fence_smem_async();
+          tc::fence_before_sync();
+          __syncthreads();
+          tc::fence_after_sync();
+          if (tid == 0) issue(k, l + 1);
+        } else {
+          tc::tmem_ld16x<3>(lane_addr, acc);
+#pragma unroll
+          for (int q = 0; q < 40; ++q) acc[q] += s_bias[4 * 64 + q];
+          epi(idx[k], idx[k] < n, acc);
+          tc::fence_before_sync();
         }
       }
-      phase ^= 1;
-      __syncthreads();  // the others learn of the finished MMA here
-      tc::fence_after_sync();
       if (failed) break;
-      float acc[64];
-      if (l < 4) {
-        tc::tmem_ld16x<4>(lane_addr, acc);
-        const float4* bb = reinterpret_cast<const float4*>(s_bias + 64 * l);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const float4 b4 = bb[k];
-          acc[4 * k] = fmaxf(acc[4 * k] + b4.x, 0.0f);
-          acc[4 * k + 1] = fmaxf(acc[4 * k + 1] + b4.y, 0.0f);
-          acc[4 * k + 2] = fmaxf(acc[4 * k + 2] + b4.z, 0.0f);
-          acc[4 * k + 3] = fmaxf(acc[4 * k + 3] + b4.w, 0.0f);
-        }
-        store_row_bf16(act[cur ^ 1], tid, acc);
-        cur ^= 1;
-      } else {
-        tc::tmem_ld16x<3>(lane_addr, acc);
-#pragma unroll
-        for (int k = 0; k < 40; ++k) acc[k] += s_bias[4 * 64 + k];
-        epi(i, i < n, acc);
-      }
-      tc::fence_before_sync();
     }
-    if (failed) break;
+    // the next pair rewrites both tiles and both accumulators
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
   }
+  // after a time-out, give MMAs still in flight a bounded chance to finish
+  // before their TMEM is freed
+  if (tid == 0)
+    for (int k = 0; k < 2; ++k)
+      if (busy[k]) tc::mbar_wait(&mbar[k], phase[k], 1u << 20);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 }  // namespace lisa

@@ -35,11 +35,16 @@ __device__ __forceinline__ void encode(const float* bmin, const float* bmax, flo
   for (int a = 0; a < 3; ++a) {
     const float ext = bmax[a] - bmin[a];
     const float u = ext > 0.0f ? fminf(fmaxf((p[a] - bmin[a]) / ext, 0.0f), 1.0f) : 0.5f;
-    float s = u * 0.125f;
+    // one sincospi, then the double-angle recurrence for the higher octaves
+    // (error ~2^k ulp at octave k: far below the inputs' BF16 precision)
+    float sn, cs;
+    sincospif(u * 0.125f, &sn, &cs);
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
-      f[3 * k + a] = sinpif(s);
-      s *= 2.0f;
+      f[3 * k + a] = sn;
+      const float s2 = 2.0f * sn * cs, c2 = (cs - sn) * (cs + sn);
+      sn = s2;
+      cs = c2;
     }
     f[36 + a] = 2.0f * u - 1.0f;
   }

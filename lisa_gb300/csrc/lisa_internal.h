@@ -106,9 +106,11 @@ struct BvhBuildResult {
 // are d_verts (3 float3 per triangle, device).  Temporaries come from `tmp`,
 // the node and leaf-triangle arrays from `out`.  With d_mat (one material
 // index per triangle, device) each leaf triangle also carries its material.
+// With refine, the binary LBVH is restructured by SAH (treelets) before the
+// 8-wide collapse.
 Status build_bvh(const float* d_verts, uint32_t num_prims, cudaStream_t stream, ScratchSource& tmp,
                  ScratchSource& out, uint4** d_nodes, float4** d_tris, BvhBuildResult* info,
-                 const int32_t* d_mat = nullptr);
+                 const int32_t* d_mat = nullptr, bool refine = true);
 // Device bytes build_bvh takes from `tmp` and from `out` for n triangles.
 size_t bvh_temp_bytes(uint32_t n);
 size_t bvh_output_bytes(uint32_t n);
@@ -191,6 +193,7 @@ struct Renderer {
   float4* guide_batch = nullptr; // guide_batch_cap x 4 training samples
   uint32_t guide_batch_cap = 0;  // samples collected per wave
   uint32_t guide_chunk = 0;      // samples per Adam step
+  uint32_t guide_max_steps = 0;  // Adam steps after the largest wave
   uint32_t max_depth = 0;
   uint64_t guide_waves_done = 0; // waves rendered in guided mode so far
   ~Renderer();

@@ -965,32 +965,45 @@ __global__ void k_brute_rays(const SceneDev* __restrict__ scd, const float* __re
 // Host view of one planned wave.
 struct WaveLaunch {
   uint32_t bounces;  // depth of its deepest scene
-  int scene;         // scene of its first group (the only one in guided mode)
-  bool train;        // guided mode: train the guide after this wave
-  bool warm;         // guided mode: warm-up wave, sample the BSDF only
+  int scene;         // scene of its first group (the only one of a guided wave)
+  bool guided;       // the guide samples this wave's bounces
+  bool train;        // guided wave: train the guide after it
+  bool warm;         // guided wave: warm-up, sample the BSDF only
+  uint32_t steps;    // guided wave: Adam steps after it, in proportion to its paths
 };
 
 namespace {
+
+// Guided mode guides the scenes with at least guide_min_spp samples per
+// pixel, one scene per wave so one network runs its inference, each wave
+// holding at most guide_spp_per_wave planes (or as many as make 1 Mi paths,
+// for small images) so the guide trains in between; the other scenes are
+// packed into plain waves after them.
+bool scene_guided(const Renderer& r, uint32_t s) {
+  return r.opts.mode == LISA_MODE_GUIDED && r.scenes[s].params.num_samples >= r.opts.guide_min_spp;
+}
 
 void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector<uint64_t>& sample_base,
                 std::vector<WaveDesc>& waves, std::vector<WaveLaunch>& wave_launch) {
   const uint32_t W = r.capacity;
   const bool per_pixel = r.opts.rng == LISA_RNG_PER_PIXEL;
-  // a guided wave serves one scene, so one network runs its inference, and
-  // holds at most guide_spp_per_wave planes so the guide trains in between
-  const bool one_scene = r.opts.mode == LISA_MODE_GUIDED;
-  const uint32_t max_planes = one_scene && r.opts.guide_spp_per_wave ? r.opts.guide_spp_per_wave : UINT32_MAX;
   waves.clear();
   wave_launch.clear();
   WaveDesc cur;
   std::memset(&cur, 0, sizeof(cur));
   uint32_t cur_b = 0;
+  bool cur_guided = false;
   auto close = [&]() {
     if (cur.num_groups == 0) return;
     cur.rng_mode = r.opts.rng;
     cur.seed = r.opts.seed;
     waves.push_back(cur);
-    wave_launch.push_back(WaveLaunch{cur_b, (int)cur.groups[0].scene, false, false});
+    // guide_steps_per_wave steps per 4 Mi paths, at least one
+    const uint32_t steps = cur_guided ? std::min<uint32_t>(r.guide_max_steps, std::max<uint32_t>(
+                                            1u, (uint32_t)(((uint64_t)cur.paths * r.opts.guide_steps_per_wave +
+                                                            (1ull << 21)) >> 22)))
+                                      : 0u;
+    wave_launch.push_back(WaveLaunch{cur_b, (int)cur.groups[0].scene, cur_guided, false, false, steps});
     std::memset(&cur, 0, sizeof(cur));
     cur_b = 0;
   };
@@ -1007,46 +1020,55 @@ void plan_waves(Renderer& r, const std::vector<uint32_t>& spp, const std::vector
     cur.acc_items += npix;
     cur_b = std::max(cur_b, r.scenes[s].params.num_bounces);
   };
-  for (uint32_t s = 0; s < r.scenes.size(); ++s) {
-    const uint32_t npix = r.scenes[s].npix;
-    uint32_t planes = spp[s];
-    uint32_t j = (uint32_t)sample_base[s];
-    if (npix == 0 || r.scenes[s].params.num_bounces == 0) continue;
-    if (one_scene) close();
-    bool scene_in_cur = false;
-    while (planes > 0) {
-      const uint32_t room = W - cur.paths;
-      if (cur.num_groups == MAX_GROUPS || (per_pixel && scene_in_cur)) {
-        close();
-        scene_in_cur = false;
-        continue;
-      }
-      if (npix <= room) {
-        uint32_t k = std::min(std::min(planes, room / npix), max_planes);
-        if (per_pixel) k = 1;
-        add(s, 0, npix, j, k);
-        scene_in_cur = true;
-        planes -= k;
-        j += k;
-        if (one_scene) {
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool one_scene = pass == 0;  // pass 0: guided scenes, pass 1: the rest
+    cur_guided = one_scene;
+    for (uint32_t s = 0; s < r.scenes.size(); ++s) {
+      if (scene_guided(r, s) != one_scene) continue;
+      const uint32_t npix = r.scenes[s].npix;
+      const uint32_t max_planes =
+          one_scene && r.opts.guide_spp_per_wave && npix
+              ? std::max<uint32_t>(r.opts.guide_spp_per_wave, ((1u << 20) + npix - 1) / npix)
+              : UINT32_MAX;
+      uint32_t planes = spp[s];
+      uint32_t j = (uint32_t)sample_base[s];
+      if (npix == 0 || r.scenes[s].params.num_bounces == 0) continue;
+      if (one_scene) close();
+      bool scene_in_cur = false;
+      while (planes > 0) {
+        const uint32_t room = W - cur.paths;
+        if (cur.num_groups == MAX_GROUPS || (per_pixel && scene_in_cur)) {
+          close();
+          scene_in_cur = false;
+          continue;
+        }
+        if (npix <= room) {
+          uint32_t k = std::min(std::min(planes, room / npix), max_planes);
+          if (per_pixel) k = 1;
+          add(s, 0, npix, j, k);
+          scene_in_cur = true;
+          planes -= k;
+          j += k;
+          if (one_scene) {
+            close();
+            scene_in_cur = false;
+          }
+        } else if (cur.paths == 0) {
+          for (uint32_t p0 = 0; p0 < npix; p0 += W) {
+            add(s, p0, std::min(W, npix - p0), j, 1);
+            close();
+          }
+          planes -= 1;
+          j += 1;
+          scene_in_cur = false;
+        } else {
           close();
           scene_in_cur = false;
         }
-      } else if (cur.paths == 0) {
-        for (uint32_t p0 = 0; p0 < npix; p0 += W) {
-          add(s, p0, std::min(W, npix - p0), j, 1);
-          close();
-        }
-        planes -= 1;
-        j += 1;
-        scene_in_cur = false;
-      } else {
-        close();
-        scene_in_cur = false;
       }
     }
+    close();
   }
-  close();
 }
 
 WaveBufs make_bufs(Renderer& r) {
@@ -1106,9 +1128,9 @@ Status guided_infer_setup() {
   return Status();
 }
 
-Status guide_collect(Renderer& r, int wave, int, cudaStream_t s) {
+Status guide_collect(Renderer& r, int wave, uint32_t cap, cudaStream_t s) {
   WaveBufs b = make_bufs(r);
-  k_guide_collect<<<r.sm_count * 8, 256, 0, s>>>(b, r.d_waves + wave, r.guide_batch, r.guide_batch_cap,
+  k_guide_collect<<<r.sm_count * 8, 256, 0, s>>>(b, r.d_waves + wave, r.guide_batch, cap,
                                                  (uint32_t)(r.guide_waves_done + (uint64_t)wave) * 2654435761u + 17u);
   LISA_CUDA(cudaGetLastError());
   return Status();
@@ -1136,12 +1158,13 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
   };
   const int acc_blocks = r.sm_count * 8;
   const bool counting = r.opts.count_traversal != 0;
-  const bool guided = r.opts.mode == LISA_MODE_GUIDED;
+  const bool guided_mode = r.opts.mode == LISA_MODE_GUIDED;
   const bool physical = r.opts.estimator == LISA_ESTIMATOR_PHYSICAL;
   for (size_t wv = 0; wv < waves.size(); ++wv) {
     const WaveDesc* wd = r.d_waves + wv;
     GuideSrc infer_src, train_src;
     GuideNet* net = nullptr;
+    const bool guided = guided_mode && waves[wv].guided;
     if (guided) {
       const SceneGpu& sg = r.scenes[waves[wv].scene];
       net = r.guides[sg.guide].get();
@@ -1178,17 +1201,20 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         else k_shade<false><<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d);
         return Status();
       }));
+      // the guide draws the bounces of the first guide_max_depth vertices
+      // of a path (0 = all); deeper ones sample the BSDF
+      const bool guided_d = guided && (r.opts.guide_max_depth == 0 || d < r.opts.guide_max_depth);
       LISA_TRY(stage(2, [&] {
         const dim3 g(r.nee_blocks), t(r.nee_threads);
         if (physical) {
-          if (guided) {
+          if (guided_d) {
             if (counting) k_nee_pb<true, true><<<g, t, 0, r.stream>>>(b, (int)d);
             else k_nee_pb<false, true><<<g, t, 0, r.stream>>>(b, (int)d);
           } else {
             if (counting) k_nee_pb<true, false><<<g, t, 0, r.stream>>>(b, (int)d);
             else k_nee_pb<false, false><<<g, t, 0, r.stream>>>(b, (int)d);
           }
-        } else if (guided) {
+        } else if (guided_d) {
           if (counting) k_nee<true, true><<<g, t, 0, r.stream>>>(b, (int)d);
           else k_nee<false, true><<<g, t, 0, r.stream>>>(b, (int)d);
         } else {
@@ -1197,11 +1223,11 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         }
         return Status();
       }));
-      if (guided) {
+      if (guided_d) {
         LISA_TRY(stage(4, [&] {
           WaveBufs bw = b;  // warm-up waves sample the BSDF only (c = 1)
           if (waves[wv].warm) bw.bsdf_fraction = 1.0f;
-          const uint32_t grid = std::min<uint32_t>((r.capacity + 127) / 128, (uint32_t)(r.sm_count * INFER_BLOCKS_PER_SM));
+          const uint32_t grid = std::min<uint32_t>((r.capacity + 255) / 256, (uint32_t)(r.sm_count * INFER_BLOCKS_PER_SM));
           if (physical)
             k_guided_infer<true><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
                                                                        bw, (int)d);
@@ -1217,9 +1243,10 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       return Status();
     }));
     if (guided && waves[wv].train) {
-      LISA_TRY(stage(4, [&] { return guide_collect(r, (int)wv, waves[wv].scene, r.stream); }));
+      const uint32_t steps = waves[wv].steps;
+      LISA_TRY(stage(4, [&] { return guide_collect(r, (int)wv, steps * r.guide_chunk, r.stream); }));
       // one Adam step per slice of the collected samples
-      for (uint32_t k = 0; k * r.guide_chunk < r.guide_batch_cap; ++k) {
+      for (uint32_t k = 0; k < steps; ++k) {
         GuideSrc slice = train_src;
         slice.first = k * r.guide_chunk;
         slice.n = (k + 1) * r.guide_chunk;
@@ -1254,10 +1281,11 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   std::vector<WaveLaunch> wb;
   plan_waves(r, spp, base, waves, wb);
   const bool guided = r.opts.mode == LISA_MODE_GUIDED;
-  // warm-up and training flags count the waves of each scene (its guide)
+  // warm-up and training flags count the guided waves of each scene (its guide)
   std::vector<uint64_t> scene_waves(r.scenes.size(), 0);
   if (guided)
     for (size_t i = 0; i < wb.size(); ++i) {
+      if (!wb[i].guided) continue;
       const uint64_t k = r.scenes[wb[i].scene].guide_waves_done + scene_waves[wb[i].scene]++;
       wb[i].train = r.opts.guide_train_waves == 0 || k < r.opts.guide_train_waves;
       wb[i].warm = k < r.opts.guide_warmup_waves;
@@ -1291,15 +1319,15 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
     // refreshed above, outside the graph
     std::vector<uint64_t> key;
     for (const WaveLaunch& w : wb)
-      key.push_back(((uint64_t)w.bounces << 32) | ((uint64_t)w.scene << 2) | ((uint64_t)w.warm << 1) | w.train);
+      key.push_back(((uint64_t)w.steps << 40) | ((uint64_t)w.bounces << 32) | ((uint64_t)w.scene << 3) |
+                    ((uint64_t)w.guided << 2) | ((uint64_t)w.warm << 1) | w.train);
     key.push_back(r.opts.count_traversal);
     key.push_back(r.opts.stage_timing);
     key.push_back((uint64_t)(uintptr_t)r.d_waves);
     if (key != r.graph_key || !r.graph_exec) {
       if (tm.on) {  // create the timing events before capture begins
         size_t need = 0;
-        const uint64_t steps = std::max<uint32_t>(1, r.opts.guide_steps_per_wave);
-        for (const WaveLaunch& w : wb) need += 2ull * (5ull * w.bounces + 6 + 2 * steps);
+        for (const WaveLaunch& w : wb) need += 2ull * (5ull * w.bounces + 6 + 2ull * w.steps);
         while (r.ev_pool.size() < need) {
           cudaEvent_t e;
           LISA_CUDA(cudaEventCreate(&e));
@@ -1380,11 +1408,13 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
     r.guide_waves_done += wb.size();
     for (size_t k = 0; k < r.scenes.size(); ++k) r.scenes[k].guide_waves_done += scene_waves[k];
     for (auto& g : r.guides) LISA_TRY(guide_check_status(*g, r.stream));
-    if (!wb.empty()) {
-      float l = 0.0f;
-      LISA_CUDA(cudaMemcpy(&l, r.guides[r.scenes[wb.back().scene].guide]->loss_last, sizeof(float),
+    for (size_t k = wb.size(); k-- > 0;) {
+      if (!wb[k].guided) continue;
+      float l = 0.0f;  // loss of the last guided wave's scene
+      LISA_CUDA(cudaMemcpy(&l, r.guides[r.scenes[wb[k].scene].guide]->loss_last, sizeof(float),
                            cudaMemcpyDeviceToHost));
       local.guide_loss = l;
+      break;
     }
   }
   local.rays_primary = hc.rays_primary;

@@ -105,7 +105,7 @@ def batch(args) -> List[dict]:
     imgs = {}
     for name, tune, opt in (("plain", tune_p, dict(seed=12, estimator=est)),
                             ("guided", tune_g, dict(seed=13, mode=G, estimator=est))):
-        o = L.apply_tuning(tune, L.default_options(**opt))
+        o = L.apply_tuning(tune, L.default_options(stage_timing=1, **opt))
         r = L.Renderer(params, o)
         r.render()  # warm-up: graph capture, guide training from scratch below
         r.close()
@@ -114,7 +114,9 @@ def batch(args) -> List[dict]:
         st = r.render()
         wall = time.perf_counter() - t0
         res[name] = dict(ms=st.ms_device, wall_s=wall, rays=st.rays, mrays_per_s=st.rays / st.ms_device / 1e3,
-                         launches=st.launches_total, tuning=tune.as_dict())
+                         launches=st.launches_total, tuning=tune.as_dict(),
+                         stages_ms={"trace": st.ms_trace, "shade": st.ms_shade, "nee": st.ms_nee,
+                                    "guide": st.ms_guide, "other": st.ms_other})
         imgs[name] = [r.image(k) for k in range(len(params))]
         r.close()
     # per-scene reference: ref_mult x the spp, plain, FP64
@@ -164,12 +166,14 @@ def summary_md(rows: List[dict], cmd: str) -> str:
         else:
             lines += [f"## batch of {r['scenes']} scenes, {r['estimator']} estimator (spp x {r['spp_scale']}, "
                       f"{r['total_paths']:,} paths)", "",
-                      "| method | device ms | Mrays/s | launches | tuning |", "|---|---|---|---|---|"]
+                      "| method | device ms | Mrays/s | launches | tuning | stage ms |", "|---|---|---|---|---|---|"]
             for m in ("plain", "guided"):
                 x = r[m]
                 t = x["tuning"]
+                sm = x.get("stages_ms", {})
                 lines.append(f"| {m} | {x['ms']:.1f} | {x['mrays_per_s']:.0f} | {x['launches']} | "
-                             f"W={t['paths_in_flight']}, {t['threads_per_block']} thr, refill {t['refill_idle']} |")
+                             f"W={t['paths_in_flight']}, {t['threads_per_block']} thr, refill {t['refill_idle']} | "
+                             + ", ".join(f"{k} {v:.0f}" for k, v in sm.items()) + " |")
             lines += ["", f"Median over scenes of guided equal-time relMSE / plain relMSE: "
                           f"{r['median_equal_time_ratio']:.3f}", "",
                       "| scene | tris | res | spp | bounces | relMSE plain | relMSE guided | guided at equal time |",

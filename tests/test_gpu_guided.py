@@ -54,7 +54,7 @@ def test_hard_indirect_guided_vs_plain(gpu, capsys):
     """Hard-indirect scene (0.02 x 0.02 light behind a baffle), 128 x 128,
     1024 spp: relMSE of plain and guided renders at the same spp against a
     32k-spp plain reference.  The guide trains online (4 warm-up waves that
-    sample the BSDF only, then 16 Adam steps per wave of 16 spp).  Training
+    sample the BSDF only, 16 Adam steps after each wave of 16 spp).  Training
     order is not deterministic (gradient atomics), so the check is a
     regression bound -- guided within 15 % of plain -- and both numbers are
     printed."""
@@ -70,10 +70,27 @@ def test_hard_indirect_guided_vs_plain(gpu, capsys):
 
     plain = L.Renderer(p, seed=12, paths_in_flight=128 * 128 * 16)
     plain.render()
+    # 16 Adam steps of 8192 samples after each 262,144-path wave
     guided = L.Renderer(p, mode=GUIDED, seed=13, paths_in_flight=128 * 128 * 16, guide_warmup_waves=4,
-                        guide_steps_per_wave=16, guide_train_batch=8192, guide_lr=3e-3)
+                        guide_steps_per_wave=256, guide_train_batch=8192, guide_lr=3e-3)
     guided.render()
     e_p, e_g = relmse(plain.image()), relmse(guided.image())
     with capsys.disabled():
         print(f"\nhard indirect 128x128 @1024 spp: relMSE plain {e_p:.6f} guided {e_g:.6f}")
     assert e_g <= 1.15 * e_p
+
+
+def test_low_spp_scenes_render_plain_in_a_guided_batch(gpu):
+    """Guided mode guides the scenes with at least guide_min_spp samples; a
+    scene below it renders on the plain path (same image as a plain
+    renderer, up to summation order) while the other is guided."""
+    a = scenes.cornell_box(width=32, height=32, num_samples=128, num_bounces=5)
+    b = scenes.icosphere_box(level=3, width=24, height=16, num_samples=8, num_bounces=6)
+    pa, pb = L.params_from_scene(a), L.params_from_scene(b)
+    guided = L.Renderer([pa, pb], mode=GUIDED, seed=4, guide_min_spp=64)
+    st = guided.render()
+    assert st.launches_guide > 0
+    plain = L.Renderer([pa, pb], seed=4)
+    plain.render()
+    np.testing.assert_allclose(guided.image(1), plain.image(1), rtol=1e-5, atol=1e-6)
+    assert not np.allclose(guided.image(0), plain.image(0), rtol=1e-5, atol=1e-6)

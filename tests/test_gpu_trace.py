@@ -97,3 +97,25 @@ def test_counting_pass(gpu):
     assert visits >= 10_000 and tests > 0
     info = r.bvh_info()
     assert info["tri_slots"] == sc.num_triangles and info["nodes"] >= 1
+
+
+@pytest.mark.gpu
+def test_sah_refinement_keeps_hits_and_cuts_traversal(gpu, oracle):
+    """The SAH treelet restructuring of the LBVH (default) against the plain
+    LBVH: closest hits stay bit-exact against the CPU BVH oracle, and the
+    traversal does less work (node visits + triangle tests per ray)."""
+    sc = scenes.icosphere_box(level=6)
+    v, _, _ = sc.soup()
+    p = L.params_from_scene(sc)
+    rays = random_rays(v, 200_000, seed=5, eye=sc.eye)
+    refined = L.Renderer(p)
+    plain = L.Renderer(p, bvh_lbvh_only=1)
+    oprim, ot = oracle.closest(v, rays, use_bvh=True)
+    for r in (refined, plain):
+        prim, t = r.trace_closest(rays)
+        _check(prim, t, oprim, ot)
+    nv_r, nt_r = refined.trace_count(rays)
+    nv_p, nt_p = plain.trace_count(rays)
+    work_r = 1.2 * nv_r + nt_r
+    work_p = 1.2 * nv_p + nt_p
+    assert work_r < work_p, (nv_r, nt_r, nv_p, nt_p)
