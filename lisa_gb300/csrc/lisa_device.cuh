@@ -147,10 +147,15 @@ __device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
   r.ox = o.x;
   r.oy = o.y;
   r.oz = o.z;
-  // __frcp_rn is the correctly rounded 1/x, the same value as 1.0f/x
-  r.ix = __frcp_rn(d.x);
-  r.iy = __frcp_rn(d.y);
-  r.iz = __frcp_rn(d.z);
+  // __frcp_rn is the correctly rounded 1/x, the same value as 1.0f/x.  A
+  // zero component takes a huge finite reciprocal of its sign instead of
+  // infinity: the node test then keeps that axis's slab (the ray's constant
+  // coordinate against the padded box) instead of turning it into NaN and
+  // dropping it, which made such rays visit most of the tree.  Only node
+  // culling reads these; the triangle test uses the shear constants.
+  r.ix = d.x != 0.0f ? __frcp_rn(d.x) : copysignf(1e30f, d.x);
+  r.iy = d.y != 0.0f ? __frcp_rn(d.y) : copysignf(1e30f, d.y);
+  r.iz = d.z != 0.0f ? __frcp_rn(d.z) : copysignf(1e30f, d.z);
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
   int kx = kz + 1;

@@ -1,7 +1,7 @@
 """Render one synthetic workload and print its statistics.
 
   python -m lisa_gb300.run --scene icosphere --res 1024 --spp 16 [--estimator physical] [--guided]
-                           [--renders 2] [--level 8]
+                           [--renders 2] [--level 8] [--width W --height H]
 
 Scenes: cornell (the procedural Cornell box), icosphere (a displaced
 icosphere of 20 * 4^level triangles, dielectric, in the box), hard_indirect
@@ -20,15 +20,16 @@ from . import scenes as S
 
 
 def make(args):
+    w, h = args.width or args.res, args.height or args.res
     if args.scene == "cornell":
-        return S.cornell_box(width=args.res, height=args.res, num_samples=args.spp, num_bounces=args.bounces or 7)
+        return S.cornell_box(width=w, height=h, num_samples=args.spp, num_bounces=args.bounces or 7)
     if args.scene == "icosphere":
-        return S.icosphere_box(level=args.level, width=args.res, height=args.res, num_samples=args.spp,
+        return S.icosphere_box(level=args.level, width=w, height=h, num_samples=args.spp,
                                num_bounces=args.bounces or 8)
     if args.scene == "hard_indirect":
-        return S.hard_indirect(level=args.level, width=args.res, height=args.res, num_samples=args.spp,
+        return S.hard_indirect(level=args.level, width=w, height=h, num_samples=args.spp,
                                num_bounces=args.bounces or 8)
-    return S.sphere_soup(n_spheres=args.spheres, width=args.res, height=args.res, num_samples=args.spp,
+    return S.sphere_soup(n_spheres=args.spheres, width=w, height=h, num_samples=args.spp,
                          num_bounces=args.bounces or 12, extent=100.0 * (args.spheres / 20000) ** (1 / 3))
 
 
@@ -38,6 +39,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m lisa_gb300.run")
     ap.add_argument("--scene", default="icosphere", choices=["cornell", "icosphere", "hard_indirect", "soup"])
     ap.add_argument("--res", type=int, default=512)
+    ap.add_argument("--width", type=int, default=0)
+    ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--spp", type=int, default=16)
     ap.add_argument("--level", type=int, default=8)
     ap.add_argument("--spheres", type=int, default=20000)
@@ -55,7 +58,7 @@ def main(argv=None):
     r = L.Renderer(L.params_from_scene(sc), opts)
     for k in range(args.renders):
         st = r.render()
-        print(json.dumps({"render": k, "scene": sc.name, "triangles": sc.num_triangles, "res": args.res,
+        print(json.dumps({"render": k, "scene": sc.name, "triangles": sc.num_triangles, "res": [sc.width, sc.height],
                           "spp": args.spp, "ms": st.ms_device, "rays": st.rays,
                           "mrays_per_s": st.rays / max(st.ms_device, 1e-9) / 1e3,
                           "stages_ms": {"trace": st.ms_trace, "shade": st.ms_shade, "nee": st.ms_nee,

@@ -151,3 +151,18 @@ def test_errors_are_status_codes(gpu):
     with pytest.raises(L.LisaError) as e:
         L.Renderer(L.params_from_scene(sc), alloc_cap_bytes=1024)
     assert e.value.code == L._native.LISA_ERR_OOM
+
+
+def test_path_by_path_sphere_soup_many_materials(gpu, oracle):
+    """Sphere soup with 1,500 materials (one per sphere, 10 % emissive):
+    per-triangle material indices beyond 8 bits, 12 bounces, both
+    estimators against the oracle path by path."""
+    sc = scenes.sphere_soup(n_spheres=1500, width=40, height=24, num_samples=2, num_bounces=12,
+                            extent=100.0 * (1500 / 20000) ** (1 / 3))
+    for est in (0, 1):
+        r = L.Renderer(L.params_from_scene(sc), estimator=est)
+        st = r.render()
+        ref, _, rays = oracle_mean(oracle, sc, estimator=est)
+        assert mismatch_fraction(r.image(), ref) <= 0.002
+        assert st.rays_primary == rays[0]
+        assert st.device_status == 0
