@@ -58,26 +58,27 @@ __device__ __forceinline__ void pack_store(uint16_t* pack, int row, int col, flo
 }
 
 // Adam (Kingma & Ba 2015) on the FP32 master parameters, fused with what
-// follows a step: the BF16 forward and transposed copies of each updated
-// weight are written in place (the zero padding rows never change), the
-// gradient is cleared for the next step and the summed loss is handed to
-// loss_last.  The step count lives on the device (the training kernel
+// surrounds a step: the gradient is the sum of the training CTAs' partial
+// gradients, the BF16 forward and transposed copies of each updated weight
+// are written in place (the zero padding rows never change), and the summed
+// loss goes to loss_last.  The step count lives on the device (the training kernel
 // increments it), so a captured graph replays with the right bias
 // correction.
 __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
-                             float* __restrict__ g, float* __restrict__ loss, float* __restrict__ loss_last,
-                             float lr, const uint32_t* __restrict__ step, uint32_t* status,
-                             uint16_t* __restrict__ pack) {
+                             const float* __restrict__ part, const float* __restrict__ loss_part, uint32_t nparts,
+                             float* __restrict__ loss_last, float lr, const uint32_t* __restrict__ step,
+                             uint32_t* status, uint16_t* __restrict__ pack) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
-    *loss_last = *loss;
-    *loss = 0.0f;
+    float l = 0.0f;
+    for (uint32_t c = 0; c < nparts; ++c) l += loss_part[c];
+    *loss_last = l;
   }
   if (i >= NPARAM) return;
   const float t = (float)max(*step, 1u);
   const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
-  const float gi = g[i];
-  g[i] = 0.0f;
+  float gi = 0.0f;  // the CTAs' partial gradients, summed in slot order
+  for (uint32_t c = 0; c < nparts; ++c) gi += part[(size_t)c * NPARAM + i];
   if (!isfinite(gi)) {
     atomicOr(status, ST_GUIDE_NONFINITE);
     return;
@@ -101,6 +102,21 @@ __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, 
 
 // ---------------------------------------------------------------------------------
 // inference: out[i][0..39] = network(features_i)
+
+// Sum of the partial gradients and losses (for callers that read them).
+__global__ void k_guide_reduce(const float* __restrict__ part, const float* __restrict__ loss_part, uint32_t nparts,
+                               float* __restrict__ grads, float* __restrict__ loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    float l = 0.0f;
+    for (uint32_t c = 0; c < nparts; ++c) l += loss_part[c];
+    *loss = l;
+  }
+  if (i >= NPARAM) return;
+  float gi = 0.0f;
+  for (uint32_t c = 0; c < nparts; ++c) gi += part[(size_t)c * NPARAM + i];
+  grads[i] = gi;
+}
 
 template <int SRC>
 __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guide_infer(const uint16_t* __restrict__ pack,
@@ -144,8 +160,8 @@ __device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int c
 
 template <int SRC>
 __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restrict__ pack, const float* __restrict__ master,
-                                                        GuideSrc src, float inv_n, float* __restrict__ grads,
-                                                        float* __restrict__ loss_out, uint32_t* status,
+                                                        GuideSrc src, float inv_n, float* __restrict__ part,
+                                                        float* __restrict__ loss_part, uint32_t* status,
                                                         uint32_t* __restrict__ step_bump) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
@@ -163,7 +179,12 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
   const uint32_t ntiles = (n - src.first + 127) / 128;
   if (step_bump && blockIdx.x == 0 && threadIdx.x == 0) *step_bump += 1;  // the Adam step that follows
-  if (blockIdx.x >= ntiles) return;
+  float* slot = part + (size_t)blockIdx.x * NPARAM;  // this CTA's partial gradient
+  if (blockIdx.x >= ntiles) {
+    for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) slot[k] = 0.0f;
+    if (threadIdx.x == 0) loss_part[blockIdx.x] = 0.0f;
+    return;
+  }
   if (tid == 0) {
     tc::mbar_init(&mbar, 1);
     failed = 0;
@@ -311,24 +332,29 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (!failed && !first && warp < 2) {
+  const bool ok = !failed && !first;
+  if (warp < 2) {
     const int o = warp * 32 + (tid & 31);
     for (int l = 0; l < 5; ++l) {
       const int rows = l < 4 ? 64 : 40;
       float d[64];
+      if (ok) {
 #pragma unroll
-      for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DW + 64 * l + lane_off + c * 16, d + c * 16);
+        for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DW + 64 * l + lane_off + c * 16, d + c * 16);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 64; ++c) d[c] = 0.0f;
+      }
       if (o < rows) {
-        float* gw = grads + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64;
-        for (int k = 0; k < 64; ++k) atomicAdd(gw + k, d[k]);
+        float4* gw = reinterpret_cast<float4*>(slot + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) gw[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
       }
     }
   }
   __syncthreads();
-  if (!failed && !first) {
-    for (int k = tid; k < 4 * 64 + 40; k += 128) atomicAdd(grads + P_B + k, s_db[k]);
-    if (tid == 0) atomicAdd(loss_out, s_loss);
-  }
+  for (int k = tid; k < 4 * 64 + 40; k += 128) slot[P_B + k] = ok ? s_db[k] : 0.0f;
+  if (tid == 0) loss_part[blockIdx.x] = ok ? s_loss : 0.0f;
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -348,6 +374,10 @@ GuideNet::~GuideNet() {
   if (loss_last) cudaFree(loss_last);
   if (status) cudaFree(status);
   if (d_step) cudaFree(d_step);
+  if (owns_part) {
+    if (grad_part) cudaFree(grad_part);
+    if (loss_part) cudaFree(loss_part);
+  }
 }
 
 namespace {
@@ -387,15 +417,33 @@ std::vector<float> guide_init(uint32_t seed) {
 
 }  // namespace
 
+static int sm_count_current() {
+  int dev = 0, sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  return sm > 0 ? sm : 1;
+}
+
+// Partial-gradient slots for `slots` training CTAs.
+Status guide_alloc_partials(float** grad_part, float** loss_part, uint32_t slots) {
+  LISA_CUDA(cudaMalloc(grad_part, sizeof(float) * (size_t)NPARAM * slots));
+  LISA_CUDA(cudaMalloc(loss_part, sizeof(float) * slots));
+  return Status();
+}
+
 Status guide_pack(GuideNet& g, cudaStream_t s) {
   k_guide_pack<<<(R_TOTAL * 64 + 255) / 256, 256, 0, s>>>(g.master, g.w_bf16);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
 
-Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s) {
+Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s, bool own_partials) {
   std::unique_ptr<GuideNet> g(new GuideNet());
   LISA_TRY(guide_alloc(*g));
+  if (own_partials) {
+    g->owns_part = true;
+    LISA_TRY(guide_alloc_partials(&g->grad_part, &g->loss_part, (uint32_t)sm_count_current()));
+  }
   std::vector<float> p = guide_init(seed);
   LISA_CUDA(cudaMemcpyAsync(g->master, p.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice, s));
   LISA_TRY(guide_pack(*g, s));
@@ -412,13 +460,6 @@ Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t 
   return Status();
 }
 
-static int sm_count_current() {
-  int dev = 0, sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
-  return sm > 0 ? sm : 1;
-}
-
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n, cudaStream_t s) {
   const uint32_t pairs = std::max<uint32_t>(1, (max_n + 255) / 256);  // two tiles of 128 per CTA
   const uint32_t grid = std::min<uint32_t>(pairs, (uint32_t)sm_count_current() * INFER_BLOCKS_PER_SM);
@@ -430,32 +471,37 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
   return Status();
 }
 
-// Gradient of one batch into g.grads and g.loss.  With zero_first the two
-// accumulators are cleared first; otherwise they must be zero already (the
-// previous Adam step leaves them so).  With adam_follows the device step
-// count advances for the Adam step launched next.
+// Gradient of one batch: every training CTA writes its partial gradient and
+// loss to its own slot of g.grad_part / g.loss_part (no atomics); the Adam
+// step (or guide_launch_reduce) sums them.  With adam_follows the device
+// step count advances for the Adam step launched next.
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s, bool zero_first, bool adam_follows) {
-  if (zero_first) {
-    LISA_CUDA(cudaMemsetAsync(g.grads, 0, sizeof(float) * NPARAM, s));
-    LISA_CUDA(cudaMemsetAsync(g.loss, 0, sizeof(float), s));
-  }
+                          cudaStream_t s, bool adam_follows) {
+  if (!g.grad_part) return Status::invalid("guide: no partial-gradient slots");
   const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
   const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
+  g.nparts = grid;
   uint32_t* bump = adam_follows ? g.d_step : nullptr;
   if (src_kind == SRC_RAW)
-    k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status,
-                                                         bump);
+    k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
+                                                         g.status, bump);
   else
-    k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grads, g.loss, g.status,
-                                                          bump);
+    k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
+                                                          g.status, bump);
+  LISA_CUDA(cudaGetLastError());
+  return Status();
+}
+
+// g.grads and g.loss = the sums of the last training launch's partials.
+Status guide_launch_reduce(GuideNet& g, cudaStream_t s) {
+  k_guide_reduce<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.grad_part, g.loss_part, g.nparts, g.grads, g.loss);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
 
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
-  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grads, g.loss, g.loss_last, lr,
-                                                    g.d_step, g.status, g.w_bf16);
+  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grad_part, g.loss_part, g.nparts,
+                                                    g.loss_last, lr, g.d_step, g.status, g.w_bf16);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
@@ -469,12 +515,10 @@ Status guide_check_status(GuideNet& g, cudaStream_t s) {
   return Status();
 }
 
-// Guided mode: one network per scene, the per-entry network outputs, the
-// per-slot training records and the training batch.
+// Guided mode: one network per scene (sharing one set of partial-gradient
+// slots), the kept training records, the emitter samples (physically based
+// estimator) and the training batch.
 Status guide_renderer_init(Renderer& r) {
-  uint32_t maxd = 1;
-  for (auto& s : r.scenes) maxd = std::max<uint32_t>(maxd, s.params.num_bounces);
-  r.max_depth = maxd;
   const uint32_t chunk = std::max<uint32_t>(128, (r.opts.guide_train_batch + 127) / 128 * 128);
   r.guide_chunk = chunk;
   // Adam steps of a wave: guide_steps_per_wave per 4 Mi paths, at least one
@@ -485,14 +529,22 @@ Status guide_renderer_init(Renderer& r) {
   if (!(r.opts.guide_bsdf_fraction >= 0.0f && r.opts.guide_bsdf_fraction <= 1.0f))
     return Status::invalid("guide_bsdf_fraction must be in [0, 1]");
   r.guides.clear();
+  const uint32_t slots = (uint32_t)sm_count_current();
+  LISA_TRY(r.arena.alloc((void**)&r.guide_grad_part, sizeof(float) * (size_t)NPARAM * slots, "guide gradients"));
+  LISA_TRY(r.arena.alloc((void**)&r.guide_loss_part, sizeof(float) * slots, "guide losses"));
   for (size_t s = 0; s < r.scenes.size(); ++s) {
     std::unique_ptr<GuideNet> g;
-    LISA_TRY(guide_create(r.opts.seed * 7919u + (uint32_t)s, g, r.stream));
+    LISA_TRY(guide_create(r.opts.seed * 7919u + (uint32_t)s, g, r.stream, false));
+    g->grad_part = r.guide_grad_part;
+    g->loss_part = r.guide_loss_part;
     r.scenes[s].guide = (int)s;
     r.guides.push_back(std::move(g));
   }
   LISA_TRY(guided_infer_setup());
-  LISA_TRY(r.arena.alloc((void**)&r.train_rec, sizeof(float4) * 5ull * maxd * r.capacity, "guide records"));
+  // kept training records: four times the batch, so that enough of them
+  // carry radiance
+  r.rec_cap = 4u * B;
+  LISA_TRY(r.arena.alloc((void**)&r.rec_list, sizeof(float4) * 5ull * r.rec_cap, "guide records"));
   if (r.opts.estimator == LISA_ESTIMATOR_PHYSICAL)
     LISA_TRY(r.arena.alloc((void**)&r.nee_light, sizeof(float4) * 2ull * r.capacity, "emitter samples"));
   LISA_TRY(r.arena.alloc((void**)&r.guide_batch, sizeof(float4) * 4ull * B, "guide batch"));
@@ -520,7 +572,7 @@ int lisa_guide_create(uint32_t seed, lisa_guide** out) {
       cudaGetLastError();
       return gret(Status(LISA_ERR_UNSUPPORTED, std::string("no CUDA device: ") + cudaGetErrorString(e)));
     }
-    Status s = guide_create(seed, g->net, g->stream);
+    Status s = guide_create(seed, g->net, g->stream, true);
     if (!s.ok()) return gret(s);
     *out = g.release();
     return gret(Status());
@@ -596,7 +648,8 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
     src.dirs = d_d;
     src.weights = d_w;
     src.n = n;
-    LISA_TRY(guide_launch_train(g->get(), src, SRC_RAW, 1.0f / (float)n, n, g->stream, true, lr > 0.0f));
+    LISA_TRY(guide_launch_train(g->get(), src, SRC_RAW, 1.0f / (float)n, n, g->stream, lr > 0.0f));
+    LISA_TRY(guide_launch_reduce(g->get(), g->stream));
     if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->get().loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     if (grads)
       LISA_CUDA(cudaMemcpyAsync(grads, g->get().grads, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, g->stream));

@@ -23,6 +23,13 @@ struct GuideNet {
   float* loss_last = nullptr; // loss of the batch of the last Adam step
   uint32_t* status = nullptr; // device status word (time-outs, non-finite values)
   uint32_t* d_step = nullptr; // Adam step count (device)
+  // per-CTA partial gradients and losses of the last training launch (one
+  // slot per CTA, summed by the Adam step); owned, or shared by a
+  // renderer's guides (their training runs one after another on its stream)
+  float* grad_part = nullptr;
+  float* loss_part = nullptr;
+  bool owns_part = false;
+  uint32_t nparts = 0;        // slots the last training launch wrote
   ~GuideNet();
 };
 
@@ -49,20 +56,24 @@ struct GuideSrc {
   float bmin[3], bmax[3];
 };
 
-Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s);
+// own_partials: allocate the network's own partial-gradient slots (a
+// renderer's guides share the renderer's instead)
+Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t s, bool own_partials);
 // Fills n training samples from the wave's guided-vertex records (host
 // launcher in wavefront.cu).
 Status guide_collect(Renderer& r, int wave, uint32_t cap, cudaStream_t s);
 // outputs: max_n x 40 floats (entries beyond the live count are not written)
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n,
                           cudaStream_t s);
-// accumulates the gradient and loss over the samples (zero_first: clear
-// them first; otherwise the previous Adam step left them zero); with
-// adam_follows the device step count advances for the next Adam step
+// one training launch: each CTA writes its partial gradient and loss to its
+// slot; with adam_follows the device step count advances for the next Adam
+// step
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s, bool zero_first, bool adam_follows);
-// Adam step; also refreshes the BF16 weights, clears the gradient and moves
-// the loss to loss_last
+                          cudaStream_t s, bool adam_follows);
+// g.grads / g.loss = sums of the last training launch's partials
+Status guide_launch_reduce(GuideNet& g, cudaStream_t s);
+// Adam step on the summed partials; also refreshes the BF16 weights and
+// moves the loss to loss_last
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s);
 Status guide_check_status(GuideNet& g, cudaStream_t s);
 Status guide_renderer_init(Renderer& r);

@@ -115,7 +115,8 @@ struct WaveCtrl {
   uint32_t head[4];
   uint32_t status;
   uint32_t guided_count;  // guided vertices of the current wave
-  uint32_t pad[2];
+  uint32_t rec_count;     // training records kept in the current wave
+  float drop_prob;        // probability of not keeping a guided vertex's record (0 = keep all)
   unsigned long long rays_primary;
   unsigned long long rays_bounce;
   unsigned long long rays_shadow;

@@ -188,13 +188,15 @@ struct Renderer {
   uint32_t graph_launches[5] = {0, 0, 0, 0, 0};  // trace, shade, nee, total, guide
   // guided mode
   std::vector<std::unique_ptr<GuideNet>> guides;
-  float4* train_rec = nullptr;   // capacity x max_depth x 5 training records
+  float4* rec_list = nullptr;    // rec_cap kept training records (5 float4 each)
+  uint32_t rec_cap = 0;
   float4* nee_light = nullptr;   // guided physically based mode: capacity x 2 emitter samples
   float4* guide_batch = nullptr; // guide_batch_cap x 4 training samples
   uint32_t guide_batch_cap = 0;  // samples collected per wave
   uint32_t guide_chunk = 0;      // samples per Adam step
   uint32_t guide_max_steps = 0;  // Adam steps after the largest wave
-  uint32_t max_depth = 0;
+  float* guide_grad_part = nullptr;  // partial-gradient slots shared by the scenes' guides
+  float* guide_loss_part = nullptr;
   uint64_t guide_waves_done = 0; // waves rendered in guided mode so far
   ~Renderer();
 };

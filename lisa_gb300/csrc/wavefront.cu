@@ -118,6 +118,7 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
     b.ctrl->head[HEAD_SHADE] = 0;
     b.ctrl->head[HEAD_NEE] = 0;
     b.ctrl->guided_count = 0;
+    b.ctrl->rec_count = 0;
     b.ctrl->train_count = 0;
     b.ctrl->rays_primary += w.paths;
   }
@@ -164,9 +165,6 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
     b.ps_att[slot] = make_float4(1.0f, 1.0f, 1.0f, b.physical ? 0.0f : __int_as_float(-1));
     b.ps_col[slot] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float((g.scene << 24) | pix));
     b.ps_rng[slot] = seed;
-    if (b.train_rec)  // guided mode: no training record yet at any depth
-      for (uint32_t d = 0; d < b.max_depth; ++d)
-        b.train_rec[5ull * ((uint64_t)slot * b.max_depth + d) + 4] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
@@ -498,6 +496,31 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
   }
 }
 
+// Appends the training record of a guided vertex with probability
+// 1 - drop_prob (decided by a hash of slot, depth and the wave's salt, not
+// by the path's stream), warp-aggregated over the lanes that call it.
+__device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, uint32_t slot, float flag, float4 r0,
+                                            float4 r1, float4 r2, float4 r3, V3 c0) {
+  const float u = (float)(tea<4>(slot * 16u + (uint32_t)depth, b.rec_salt) >> 8) * (1.0f / 16777216.0f);
+  const bool keep = u >= b.ctrl->drop_prob;
+  const uint32_t active = __activemask();
+  const uint32_t mask = __ballot_sync(active, keep);
+  if (!mask) return;
+  const int leader = __ffs(mask) - 1;
+  const int lane = threadIdx.x & 31;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&b.ctrl->rec_count, (uint32_t)__popc(mask));
+  base = __shfl_sync(active, base, leader);
+  const uint32_t k = base + __popc(mask & lanemask_lt());
+  if (!keep || k >= b.rec_cap) return;
+  float4* rec = b.rec_list + 5ull * k;
+  rec[0] = r0;
+  rec[1] = r1;
+  rec[2] = r2;
+  rec[3] = r3;
+  rec[4] = make_float4(c0.x, c0.y, c0.z, __uint_as_float((slot << 1) | (flag != 0.0f ? 1u : 0u)));
+}
+
 // ---------------------------------------------------------------------------
 // Guided bounces, in the epilogue of the guide's inference (k_guided_infer):
 // thread t holds the 40 network outputs of emitter-queue entry i in
@@ -525,12 +548,9 @@ __device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int dept
   nd = guided_bounce(o, N, seed, b.bsdf_fraction, weight);
   const V3 att = ld3(at) * weight;
   const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-  float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + depth);
-  rec[0] = make_float4(p.x, p.y, p.z, weight);
-  rec[1] = make_float4(N.x, N.y, N.z, nd.x);
-  rec[2] = make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y);
-  rec[3] = make_float4(att.x, att.y, att.z, nd.z);
-  rec[4] = make_float4(cw.x, cw.y, cw.z, stale >= 0 ? 2.0f : 1.0f);  // 0 = no record
+  keep_record(b, depth, slot, stale >= 0 ? 1.0f : 0.0f, make_float4(p.x, p.y, p.z, weight),
+              make_float4(N.x, N.y, N.z, nd.x), make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y),
+              make_float4(att.x, att.y, att.z, nd.z), ld3(cw));
   b.ps_rng[slot] = seed;
   b.ps_att[slot] = make_float4(att.x, att.y, att.z, at.w);
   ++guided_n;
@@ -730,12 +750,8 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
     prev = r * qm;
     want = depth + 1 < (int)sc.num_bounces && weight > 0.0f;
     const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-    float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + depth);
-    rec[0] = make_float4(p.x, p.y, p.z, weight);
-    rec[1] = make_float4(N.x, N.y, N.z, nd.x);
-    rec[2] = make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y);
-    rec[3] = make_float4(att.x, att.y, att.z, nd.z);
-    rec[4] = make_float4(col.x, col.y, col.z, 1.0f);  // flag feature 0
+    keep_record(b, depth, slot, 0.0f, make_float4(p.x, p.y, p.z, weight), make_float4(N.x, N.y, N.z, nd.x),
+                make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y), make_float4(att.x, att.y, att.z, nd.z), col);
     ++guided_n;
   } else {
     nd = reflect(D, Ns);
@@ -826,57 +842,54 @@ __global__ void k_accumulate(WaveBufs b, const WaveDesc* __restrict__ wave) {
 }
 
 // ---------------------------------------------------------------------------
-// guide training samples from the wave's guided vertices
+// guide training samples from the wave's kept records
 //
 // Each record holds the radiance the path had gathered when the vertex was
 // left (c0) and the throughput after its bounce (a1); with the path's final
 // radiance c, the radiance that arrived along the sampled direction is
 // L = (c - c0) / a1.  The training weight is mean(L) * p_bsdf / q, the
-// importance weight of the Neural Importance Sampling loss.  About `cap`
-// samples are kept, uniformly at random over the wave.
+// importance weight of the Neural Importance Sampling loss; records with
+// weight 0 carry no gradient and are skipped.  At most `cap` samples go to
+// the batch.  The keep probability of the next wave's records is set from
+// this wave's guided-vertex count, aiming at 90 % of the record capacity.
 
-__global__ void k_guide_collect(WaveBufs b, const WaveDesc* __restrict__ wave, float4* __restrict__ batch,
-                                uint32_t cap, uint32_t salt) {
-  const WaveDesc& w = *wave;
+__global__ void k_guide_collect(WaveBufs b, float4* __restrict__ batch, uint32_t cap) {
   const uint32_t total = *(volatile uint32_t*)&b.ctrl->guided_count;
-  const float keep = total > cap ? (float)cap / (float)total : 1.0f;
+  const uint32_t nrec = min(*(volatile uint32_t*)&b.ctrl->rec_count, b.rec_cap);
   const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t end = (w.paths + 31u) & ~31u;
-  for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < end; slot += stride) {
-    const bool live = slot < w.paths;
-    const float4 col = live ? b.ps_col[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (uint32_t d = 0; d < b.max_depth; ++d) {
-      bool want = false;
-      float4 r0, r1, r2, r3;
-      float wt = 0.0f, flag = 0.0f;
-      if (live) {
-        const float4* rec = b.train_rec + 5ull * ((uint64_t)slot * b.max_depth + d);
-        const float4 r4 = rec[4];
-        if (r4.w != 0.0f) {
-          flag = r4.w - 1.0f;
-          r0 = rec[0];
-          r1 = rec[1];
-          r2 = rec[2];
-          r3 = rec[3];
-          float l = 0.0f;
-          int nl = 0;
-          if (r3.x > 0.0f) { l += (col.x - r4.x) / r3.x; ++nl; }
-          if (r3.y > 0.0f) { l += (col.y - r4.y) / r3.y; ++nl; }
-          if (r3.z > 0.0f) { l += (col.z - r4.z) / r3.z; ++nl; }
-          wt = nl ? l / (float)nl * r0.w : 0.0f;
-          const float u = (float)(tea<4>(slot * 16u + d, salt) >> 8) * (1.0f / 16777216.0f);
-          want = wt > 0.0f && isfinite(wt) && u < keep;
-        }
-      }
-      const uint32_t i = warp_reserve(&b.ctrl->train_count, want);
-      if (want && i < cap) {
-        float4* o = batch + 4ull * i;
-        o[0] = make_float4(r0.x, r0.y, r0.z, r1.x);
-        o[1] = make_float4(r1.y, r1.z, r2.x, r2.y);
-        o[2] = make_float4(r2.z, r1.w, r2.w, r3.w);
-        o[3] = make_float4(fminf(wt, 1e4f), flag, 0.0f, 0.0f);
-      }
+  const uint32_t end = (nrec + 31u) & ~31u;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < end; k += stride) {
+    bool want = false;
+    float4 r0, r1, r2, r3, r4;
+    float wt = 0.0f;
+    if (k < nrec) {
+      const float4* rec = b.rec_list + 5ull * k;
+      r0 = rec[0];
+      r1 = rec[1];
+      r2 = rec[2];
+      r3 = rec[3];
+      r4 = rec[4];
+      const float4 col = b.ps_col[__float_as_uint(r4.w) >> 1];
+      float l = 0.0f;
+      int nl = 0;
+      if (r3.x > 0.0f) { l += (col.x - r4.x) / r3.x; ++nl; }
+      if (r3.y > 0.0f) { l += (col.y - r4.y) / r3.y; ++nl; }
+      if (r3.z > 0.0f) { l += (col.z - r4.z) / r3.z; ++nl; }
+      wt = nl ? l / (float)nl * r0.w : 0.0f;
+      want = wt > 0.0f && isfinite(wt);
     }
+    const uint32_t i = warp_reserve(&b.ctrl->train_count, want);
+    if (want && i < cap) {
+      float4* o = batch + 4ull * i;
+      o[0] = make_float4(r0.x, r0.y, r0.z, r1.x);
+      o[1] = make_float4(r1.y, r1.z, r2.x, r2.y);
+      o[2] = make_float4(r2.z, r1.w, r2.w, r3.w);
+      o[3] = make_float4(fminf(wt, 1e4f), (float)(__float_as_uint(r4.w) & 1u), 0.0f, 0.0f);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const float keep = total ? fminf(1.0f, 0.9f * (float)b.rec_cap / (float)total) : 1.0f;
+    b.ctrl->drop_prob = 1.0f - keep;
   }
 }
 
@@ -1090,9 +1103,9 @@ WaveBufs make_bufs(Renderer& r) {
   b.capacity = r.capacity;
   b.refill_busy_max = 32u - (r.opts.refill_idle ? std::min<uint32_t>(r.opts.refill_idle, 32u) : LISA_REFILL_IDLE);
   b.physical = r.opts.estimator == LISA_ESTIMATOR_PHYSICAL;
-  b.train_rec = r.train_rec;
+  b.rec_list = r.rec_list;
+  b.rec_cap = r.rec_cap;
   b.nee_light = r.nee_light;
-  b.max_depth = r.max_depth;
   b.bsdf_fraction = r.opts.guide_bsdf_fraction;
   return b;
 }
@@ -1128,10 +1141,9 @@ Status guided_infer_setup() {
   return Status();
 }
 
-Status guide_collect(Renderer& r, int wave, uint32_t cap, cudaStream_t s) {
+Status guide_collect(Renderer& r, int, uint32_t cap, cudaStream_t s) {
   WaveBufs b = make_bufs(r);
-  k_guide_collect<<<r.sm_count * 8, 256, 0, s>>>(b, r.d_waves + wave, r.guide_batch, cap,
-                                                 (uint32_t)(r.guide_waves_done + (uint64_t)wave) * 2654435761u + 17u);
+  k_guide_collect<<<r.sm_count * 8, 256, 0, s>>>(b, r.guide_batch, cap);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
@@ -1227,6 +1239,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         LISA_TRY(stage(4, [&] {
           WaveBufs bw = b;  // warm-up waves sample the BSDF only (c = 1)
           if (waves[wv].warm) bw.bsdf_fraction = 1.0f;
+          bw.rec_salt = (uint32_t)(r.guide_waves_done + wv) * 2654435761u + 17u;
           const uint32_t grid = std::min<uint32_t>((r.capacity + 255) / 256, (uint32_t)(r.sm_count * INFER_BLOCKS_PER_SM));
           if (physical)
             k_guided_infer<true><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
@@ -1252,7 +1265,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         slice.n = (k + 1) * r.guide_chunk;
         LISA_TRY(stage(4, [&] {
           return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream,
-                                    false, true);
+                                    true);
         }));
         LISA_TRY(stage(4, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream); }));
       }

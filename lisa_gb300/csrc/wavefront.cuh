@@ -23,15 +23,17 @@ struct WaveBufs {
   uint32_t refill_busy_max;  // persistent kernels refill a warp once at most this many lanes are busy
   uint32_t physical;         // physically based estimator: ps_att.w = pdf of the last diffuse bounce
   // guided mode (null otherwise)
-  float4* train_rec;  // per slot and depth: 5 float4 training record
+  float4* rec_list;   // kept training records, 5 float4 each (see below)
+  uint32_t rec_cap;   // records rec_list holds
+  uint32_t rec_salt;  // per-wave salt of the keep decision
   float4* nee_light;  // guided physically based mode: per entry, the emitter sample (2 float4)
-  uint32_t max_depth;
   float bsdf_fraction;  // one-sample MIS: probability of the BSDF strategy
 };
 
-// Training record of one guided vertex (5 float4, slot-major, depth-minor):
+// Training record of one kept guided vertex (5 float4, appended to rec_list):
 //   (p.xyz, weight = p_bsdf/q)  (N.xyz, w.x)  (view.xyz, w.y)
-//   (throughput after the bounce .xyz, w.z)  (radiance so far .xyz, valid)
+//   (throughput after the bounce .xyz, w.z)
+//   (radiance so far .xyz, bits: slot << 1 | emitter flag)
 
 struct GuideSampling {
   float bsdf_fraction;  // c in q = c p_bsdf + (1-c) p_guide
