@@ -13,6 +13,11 @@ the data path; a barrier and a max-reduce of the time only).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
+The line also carries `quality`: the equal-time relMSE of MLP-guided vs
+plain sampling on the hard-indirect scene (1024 x 1024, 256 spp, physically
+based estimator) against a 4,096-spp FP64 reference, measured in the same
+run after the timed region.
+
 --impl reference times the reference estimator's CPU restatement (the
 oracle: LiSA's own GPU path is OptiX and does not build here) on all host
 cores, on a bounded sample of the same workload.
@@ -304,6 +309,22 @@ def run_ours(args, rank, ws, local):
             e2e_t += dt
     e2e_val = sum_over_ranks(float(e2e_rays), ws) / max(max_over_ranks(e2e_t, ws), 1e-9) / 1e6
     info = r.bvh_info()
+    # equal-time relMSE of guided vs plain sampling (hard-indirect scene,
+    # 1024x1024, 256 spp, physically based estimator) against a 4,096-spp
+    # FP64 reference whose own variance is removed from the figures
+    quality = None
+    if rank == 0 and not (args.quick or args.no_quality):
+        from lisa_gb300 import study
+
+        qa = argparse.Namespace(res=1024, level=8, spp=256, ref_spp=4096, ref_chunk=256, estimator="physical")
+        q = study.hard_indirect(qa)[0]
+        quality = {"workload": "hard-indirect scene (C2 mesh, 0.02 light behind a baffle), 1024x1024, 256 spp, "
+                               "physically based estimator",
+                   "reference": "4096 spp plain, FP64 accumulation; relMSE with its variance removed",
+                   "relmse_plain": q["plain"]["relmse_corrected"], "relmse_guided": q["guided"]["relmse_corrected"],
+                   "ms_plain": q["plain"]["ms"], "ms_guided": q["guided"]["ms"],
+                   "equal_time_relmse_guided_over_plain": q["equal_time_relmse"]["guided"] / q["equal_time_relmse"]["plain"],
+                   "guided_time_to_plain_error": q["time_to_plain_error"]}
     cpu = None
     if rank == 0 and not (args.no_cpu or args.quick):
         cv, cdesc, ccores = cpu_sample(sc, spp=args.spp_per_step, budget_s=args.cpu_budget)
@@ -341,6 +362,7 @@ def run_ours(args, rank, ws, local):
                     "what": "Renderer create (H2D soup + GPU BVH build) + 16-spp render + FP32 image D2H"},
             "clocks": clocks,
             "gpu_launches": int(launches),
+            "quality": quality,
         }
         print(json.dumps(line), flush=True)
 
@@ -357,7 +379,8 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--res", type=int, default=1024, help="square resolution (profiling cases use less)")
-    ap.add_argument("--quick", action="store_true", help="skip the CPU baseline and the end-to-end leg")
+    ap.add_argument("--quick", action="store_true", help="skip the CPU baseline, the end-to-end leg and the quality leg")
+    ap.add_argument("--no-quality", action="store_true", help="skip the guided-vs-plain relMSE leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -114,7 +114,8 @@ typedef struct lisa_options {
   /* path guide (LISA_MODE_GUIDED) */
   float guide_bsdf_fraction; /* probability c of sampling the BSDF strategy    */
   float guide_lr;            /* Adam learning rate                             */
-  uint32_t guide_train_batch;/* training samples per wave (multiple of 128)    */
+  uint32_t guide_train_batch;/* samples per Adam step (multiple of 128; 0 = one
+                                128-sample tile per SM)                        */
   uint32_t guide_train_waves;/* waves that train (0 = every wave)              */
   uint64_t alloc_cap_bytes;  /* refuse device allocations beyond this (0=none) */
   uint32_t count_traversal;  /* run the counting variants of the traversal
@@ -140,7 +141,8 @@ typedef struct lisa_options {
   uint32_t guide_max_depth;  /* the guide draws the bounces of the first this
                                 many vertices of a path; deeper ones sample
                                 the BSDF (0 = every vertex)                  */
-  uint32_t reserved;
+  uint32_t guide_train_steps;/* Adam steps per scene, after which its guide
+                                stays fixed (0 = no limit)                   */
 } lisa_options;
 
 /* Per-call statistics.  Ray counts are rays actually traced: primary +

@@ -69,7 +69,7 @@ class Options(C.Structure):
                 ("guide_warmup_waves", C.c_uint32), ("guide_steps_per_wave", C.c_uint32),
                 ("guide_spp_per_wave", C.c_uint32), ("refill_idle", C.c_uint32),
                 ("estimator", C.c_uint32), ("bvh_lbvh_only", C.c_uint32), ("guide_min_spp", C.c_uint32),
-                ("guide_max_depth", C.c_uint32), ("reserved", C.c_uint32)]
+                ("guide_max_depth", C.c_uint32), ("guide_train_steps", C.c_uint32)]
 
 
 class RenderStats(C.Structure):

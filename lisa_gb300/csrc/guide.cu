@@ -148,14 +148,34 @@ __device__ __forceinline__ uint32_t at_offset(uint32_t m, uint32_t b) {
   return (b >> 6) * (uint32_t)TILE + tc::sw128_offset(m, b & 63u);
 }
 
-__device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int count) {
-  // column sums over the block: warp shuffle reduction, then shared atomics
-  for (int k = 0; k < count; ++k) {
-    float x = v[k];
+// One halving round of a warp reduce-scatter: the lane keeps the upper or
+// lower half of its n values (by lane bit m) plus the partner's same half.
+template <int N>
+__device__ __forceinline__ void reduce_scatter_round(const float* in, float* out, int m) {
+  const bool up = (threadIdx.x & m) != 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&s_db[k], x);
+  for (int k = 0; k < N / 2; ++k) {
+    const float send = up ? in[k] : in[k + N / 2];
+    const float keep = up ? in[k + N / 2] : in[k];
+    out[k] = keep + __shfl_xor_sync(0xffffffffu, send, m);
   }
+}
+
+// Column sums of the warp's 32 rows of v[64] added to s_db[0 .. count):
+// a reduce-scatter by recursive halving leaves each lane two of the 64
+// column sums, which it adds with shared-memory atomics.
+__device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int count) {
+  float a[32], b[16], c[8], d[4], e[2];
+  reduce_scatter_round<64>(v, a, 16);
+  reduce_scatter_round<32>(a, b, 8);
+  reduce_scatter_round<16>(b, c, 4);
+  reduce_scatter_round<8>(c, d, 2);
+  reduce_scatter_round<4>(d, e, 1);
+  const int lane = threadIdx.x & 31;
+  const int col = ((lane & 16) ? 32 : 0) + ((lane & 8) ? 16 : 0) + ((lane & 4) ? 8 : 0) + ((lane & 2) ? 4 : 0) +
+                  ((lane & 1) ? 2 : 0);
+  if (col < count) atomicAdd(&s_db[col], e[0]);
+  if (col + 1 < count) atomicAdd(&s_db[col + 1], e[1]);
 }
 
 template <int SRC>
@@ -173,6 +193,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   __shared__ float s_db[4 * 64 + 40];
+  __shared__ __align__(16) float s_b[4 * 64 + 48];  // biases
   __shared__ float s_loss;
   const int tid = threadIdx.x, warp = tid >> 5;
   // samples [src.first, n)
@@ -193,6 +214,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   for (int c = tid; c < PACK_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
+  for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
   tc::fence_smem_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -247,13 +269,20 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
       if (tid == 0) issue_layer(tmem + TM_FWD, act + l * TILE, w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, N, &mbar);
       wait_mma();
       if (failed) break;
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (c * 16 < (int)N) tc::tmem_ld16(tmem + TM_FWD + lane_off + c * 16, v + c * 16);
       if (l < 4) {
+        tc::tmem_ld16x<4>(tmem + TM_FWD + lane_off, v);
+        const float4* bb = reinterpret_cast<const float4*>(s_b + 64 * l);
 #pragma unroll
-        for (int k = 0; k < 64; ++k) v[k] = fmaxf(v[k] + __ldg(master + P_B + 64 * l + k), 0.0f);
+        for (int q = 0; q < 16; ++q) {
+          const float4 b4 = bb[q];
+          v[4 * q] = fmaxf(v[4 * q] + b4.x, 0.0f);
+          v[4 * q + 1] = fmaxf(v[4 * q + 1] + b4.y, 0.0f);
+          v[4 * q + 2] = fmaxf(v[4 * q + 2] + b4.z, 0.0f);
+          v[4 * q + 3] = fmaxf(v[4 * q + 3] + b4.w, 0.0f);
+        }
         store_row_bf16(act + (l + 1) * TILE, tid, v);
+      } else {
+        tc::tmem_ld16x<3>(tmem + TM_FWD + lane_off, v);
       }
       tc::fence_before_sync();
     }
@@ -263,7 +292,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
     {
       float o[40];
 #pragma unroll
-      for (int k = 0; k < 40; ++k) o[k] = v[k] + __ldg(master + P_B5 + k);
+      for (int k = 0; k < 40; ++k) o[k] = v[k] + s_b[4 * 64 + k];
       float lsum = 0.0f;
       if (valid && wt != 0.0f) {
         const float il = rsqrtf(fmaxf(wx * wx + wy * wy + wz * wz, 1e-30f));
@@ -318,8 +347,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
       if (l > 0) {
         float h[64];
         load_row_bf16(act + l * TILE, tid, h);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DH + lane_off + c * 16, g + c * 16);
+        tc::tmem_ld16x<4>(tmem + TM_DH + lane_off, g);
 #pragma unroll
         for (int k = 0; k < 64; ++k) g[k] = h[k] > 0.0f ? g[k] : 0.0f;
         add_bias_grad(s_db + 64 * (l - 1), g, 64);
@@ -519,7 +547,9 @@ Status guide_check_status(GuideNet& g, cudaStream_t s) {
 // slots), the kept training records, the emitter samples (physically based
 // estimator) and the training batch.
 Status guide_renderer_init(Renderer& r) {
-  const uint32_t chunk = std::max<uint32_t>(128, (r.opts.guide_train_batch + 127) / 128 * 128);
+  // samples per Adam step: a multiple of 128; 0 = one 128-sample tile per SM
+  const uint32_t chunk = r.opts.guide_train_batch ? std::max<uint32_t>(128, (r.opts.guide_train_batch + 127) / 128 * 128)
+                                                  : 128u * (uint32_t)sm_count_current();
   r.guide_chunk = chunk;
   // Adam steps of a wave: guide_steps_per_wave per 4 Mi paths, at least one
   r.guide_max_steps = std::max<uint32_t>(

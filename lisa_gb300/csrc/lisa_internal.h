@@ -150,6 +150,7 @@ struct SceneGpu {
   float eye[3], U[3], V[3], W[3];
   int guide = -1;
   uint64_t guide_waves_done = 0;  // guided waves of this scene so far
+  uint64_t guide_steps_done = 0;  // Adam steps of its guide so far
 };
 
 struct Renderer {

@@ -501,6 +501,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
 // by the path's stream), warp-aggregated over the lanes that call it.
 __device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, uint32_t slot, float flag, float4 r0,
                                             float4 r1, float4 r2, float4 r3, V3 c0) {
+  if (b.rec_cap == 0) return;  // a wave that does not train keeps no records
   const float u = (float)(tea<4>(slot * 16u + (uint32_t)depth, b.rec_salt) >> 8) * (1.0f / 16777216.0f);
   const bool keep = u >= b.ctrl->drop_prob;
   const uint32_t active = __activemask();
@@ -1240,6 +1241,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
           WaveBufs bw = b;  // warm-up waves sample the BSDF only (c = 1)
           if (waves[wv].warm) bw.bsdf_fraction = 1.0f;
           bw.rec_salt = (uint32_t)(r.guide_waves_done + wv) * 2654435761u + 17u;
+          if (!waves[wv].train) bw.rec_cap = 0;
           const uint32_t grid = std::min<uint32_t>((r.capacity + 255) / 256, (uint32_t)(r.sm_count * INFER_BLOCKS_PER_SM));
           if (physical)
             k_guided_infer<true><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
@@ -1294,13 +1296,22 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   std::vector<WaveLaunch> wb;
   plan_waves(r, spp, base, waves, wb);
   const bool guided = r.opts.mode == LISA_MODE_GUIDED;
-  // warm-up and training flags count the guided waves of each scene (its guide)
-  std::vector<uint64_t> scene_waves(r.scenes.size(), 0);
+  // warm-up and training flags count the guided waves of each scene (its
+  // guide); a scene's Adam steps stop at guide_train_steps
+  std::vector<uint64_t> scene_waves(r.scenes.size(), 0), scene_steps(r.scenes.size(), 0);
   if (guided)
     for (size_t i = 0; i < wb.size(); ++i) {
       if (!wb[i].guided) continue;
-      const uint64_t k = r.scenes[wb[i].scene].guide_waves_done + scene_waves[wb[i].scene]++;
-      wb[i].train = r.opts.guide_train_waves == 0 || k < r.opts.guide_train_waves;
+      const int sc = wb[i].scene;
+      const uint64_t k = r.scenes[sc].guide_waves_done + scene_waves[sc]++;
+      const uint64_t done = r.scenes[sc].guide_steps_done + scene_steps[sc];
+      if (r.opts.guide_train_steps)
+        wb[i].steps = (uint32_t)std::min<uint64_t>(wb[i].steps, done < r.opts.guide_train_steps
+                                                                    ? r.opts.guide_train_steps - done
+                                                                    : 0);
+      wb[i].train = (r.opts.guide_train_waves == 0 || k < r.opts.guide_train_waves) && wb[i].steps > 0;
+      if (!wb[i].train) wb[i].steps = 0;
+      scene_steps[sc] += wb[i].steps;
       wb[i].warm = k < r.opts.guide_warmup_waves;
     }
   if (waves.size() > r.wave_capacity) {
@@ -1419,7 +1430,10 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   }
   if (guided) {
     r.guide_waves_done += wb.size();
-    for (size_t k = 0; k < r.scenes.size(); ++k) r.scenes[k].guide_waves_done += scene_waves[k];
+    for (size_t k = 0; k < r.scenes.size(); ++k) {
+      r.scenes[k].guide_waves_done += scene_waves[k];
+      r.scenes[k].guide_steps_done += scene_steps[k];
+    }
     for (auto& g : r.guides) LISA_TRY(guide_check_status(*g, r.stream));
     for (size_t k = wb.size(); k-- > 0;) {
       if (!wb[k].guided) continue;
