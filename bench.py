@@ -237,7 +237,18 @@ def run_ours(args, rank, ws, local):
     # each rank renders its own range of sample indices of the frame
     # (lisa_gb300.shard); one rank renders samples 0, 1, 2, ...
     shard_first = rank * (1 << 20)
-    opts = L.default_options(stage_timing=1, paths_in_flight=args.paths)
+    # queue and block sizes from the autotuner (short renders of this
+    # workload, before and outside the timed region)
+    tuning = None
+    base = L.default_options(paths_in_flight=args.paths)
+    if not args.no_tune:
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as td:
+            tuning = L.autotune(params, base, cache=os.path.join(td, "tune.json"))
+        base = L.apply_tuning(tuning, base)
+    tuned = {k: getattr(base, k) for k in ("paths_in_flight", "threads_per_block", "blocks_per_sm", "refill_idle")}
+    opts = L.default_options(stage_timing=1, **tuned)
     r = L.Renderer(params, opts)
     r.set_sample_offset(shard_first)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -272,7 +283,7 @@ def run_ours(args, rank, ws, local):
     other_ms = sum(s.ms_other for s in stats)
     launches = sum(s.launches_total for s in stats)
     # counting pass (same seeds, one step) for the algorithmic bytes per launch
-    copts = L.default_options(paths_in_flight=args.paths, count_traversal=1)
+    copts = L.default_options(count_traversal=1, **tuned)
     rc = L.Renderer(params, copts)
     rc.set_sample_offset(shard_first)
     cs = rc.render_progressive(args.spp_per_step)
@@ -298,7 +309,7 @@ def run_ours(args, rank, ws, local):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         p2 = L.params_from_arrays(v, n, mi, mats, sc.width, sc.height, sc.eye, sc.look_at, sc.fov, 256, 8)
-        r2 = L.Renderer(p2, L.default_options(paths_in_flight=args.paths))
+        r2 = L.Renderer(p2, L.default_options(**tuned))
         r2.set_sample_offset(shard_first + (i + 1) * 4096)
         s2 = r2.render_progressive(args.spp_per_step)
         img = r2.image()
@@ -337,6 +348,8 @@ def run_ours(args, rank, ws, local):
             "config": {"workload": WORKLOAD, "triangles": sc.num_triangles, "width": sc.width,
                        "height": sc.height, "spp_per_step": args.spp_per_step, "bounces": sc.num_bounces,
                        "paths_in_flight": r.options.paths_in_flight or None,
+                       "tuning": None if tuning is None else {**tuned, "candidates": tuning.candidates,
+                                                               "probe_mrays_per_s": tuning.mrays_per_s},
                        "l2": "working set > L2 (BVH+triangles+queues) and a 256 MB L2 flush before every step",
                        "bvh": info, "sharding": "disjoint sample ranges per rank"},
             "roofline": {"bound": "hbm", "kernel": "k_nee (emitter search + bounce)", "achieved": achieved,
@@ -381,6 +394,7 @@ def main():
     ap.add_argument("--res", type=int, default=1024, help="square resolution (profiling cases use less)")
     ap.add_argument("--quick", action="store_true", help="skip the CPU baseline, the end-to-end leg and the quality leg")
     ap.add_argument("--no-quality", action="store_true", help="skip the guided-vs-plain relMSE leg")
+    ap.add_argument("--no-tune", action="store_true", help="library default queue and block sizes")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -41,12 +41,12 @@ def test_guided_estimator_is_unbiased(gpu):
 def test_guide_trains_during_render(gpu):
     sc = scenes.cornell_box(width=32, height=32, num_samples=64, num_bounces=5)
     r = L.Renderer(L.params_from_scene(sc), mode=GUIDED, seed=3, guide_train_batch=4096,
-                   paths_in_flight=32 * 32 * 4)
+                   paths_in_flight=32 * 32 * 4, guide_min_spp=0)
     g = r.guide()
     before = g.params().copy()
     st = r.render()
     after = g.params()
-    assert st.launches_guide >= 16  # one training step per wave, 16 waves
+    assert st.launches_guide >= 16  # inference and training launches over 16 waves
     assert np.isfinite(after).all() and not np.array_equal(before, after)
 
 
