@@ -178,6 +178,7 @@ struct Renderer {
   // launch shapes
   int trace_blocks = 0, trace_threads = 128;
   int nee_blocks = 0, nee_threads = 128;
+  int nee_pb_blocks = 0;  // physically based emitter kernel
   int shade_blocks = 0, shade_threads = 256;
   // events for stage timing
   std::vector<cudaEvent_t> ev_pool;

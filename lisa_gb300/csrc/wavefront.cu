@@ -38,7 +38,10 @@ namespace lisa {
 constexpr uint32_t FULL = 0xffffffffu;
 
 #ifndef LISA_NEE_MIN_BLOCKS
-#define LISA_NEE_MIN_BLOCKS 7  // 7 x 128 threads per SM (72 registers)
+#define LISA_NEE_MIN_BLOCKS 8  // 8 x 128 threads per SM (64 registers; measured best of 6..10)
+#endif
+#ifndef LISA_NEE_PB_MIN_BLOCKS
+#define LISA_NEE_PB_MIN_BLOCKS 7  // physically based emitter kernel: 7 x 128 threads per SM
 #endif
 #ifndef LISA_REFILL_IDLE
 #define LISA_REFILL_IDLE 12  // default: idle lanes (of 32) that trigger a refill round
@@ -574,7 +577,7 @@ __device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int dept
 // and draws the bounce once the guide's inference has run.
 
 template <bool COUNT, bool SPLIT>
-__global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee_pb(WaveBufs b, int depth) {
+__global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->nee_count;
   const int lane = threadIdx.x & 31;
@@ -1218,7 +1221,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       // of a path (0 = all); deeper ones sample the BSDF
       const bool guided_d = guided && (r.opts.guide_max_depth == 0 || d < r.opts.guide_max_depth);
       LISA_TRY(stage(2, [&] {
-        const dim3 g(r.nee_blocks), t(r.nee_threads);
+        const dim3 g(physical ? r.nee_pb_blocks : r.nee_blocks), t(r.nee_threads);
         if (physical) {
           if (guided_d) {
             if (counting) k_nee_pb<true, true><<<g, t, 0, r.stream>>>(b, (int)d);
@@ -1598,6 +1601,11 @@ Status configure_launch(Renderer& r) {
   bps = std::min(bps, std::max(occ, 1));
   r.nee_threads = tthreads;
   r.nee_blocks = r.sm_count * bps;
+  // the physically based emitter kernel has its own register budget
+  LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_nee_pb<false, false>, tthreads, 0));
+  bps = r.opts.blocks_per_sm ? (int)r.opts.blocks_per_sm : std::max(occ, 1);
+  bps = std::min(bps, std::max(occ, 1));
+  r.nee_pb_blocks = r.sm_count * bps;
   LISA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_shade<false>, 256, 0));
   r.shade_threads = 256;
   r.shade_blocks = r.sm_count * std::max(occ, 1);
