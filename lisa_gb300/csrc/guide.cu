@@ -68,17 +68,25 @@ __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, 
                              const float* __restrict__ part, const float* __restrict__ loss_part, uint32_t nparts,
                              float* __restrict__ loss_last, float lr, const uint32_t* __restrict__ step,
                              uint32_t* status, uint16_t* __restrict__ pack) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) {
+  // four threads per parameter (neighbouring lanes) each sum every fourth
+  // partial slot; the sums meet by shuffles
+  const int t4 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t4 >> 2, q = t4 & 3;
+  if (t4 == 0) {
     float l = 0.0f;
     for (uint32_t c = 0; c < nparts; ++c) l += loss_part[c];
     *loss_last = l;
   }
-  if (i >= NPARAM) return;
+  float gi = 0.0f;
+  if (i < NPARAM) {
+#pragma unroll 8
+    for (uint32_t c = q; c < nparts; c += 4) gi += part[(size_t)c * NPARAM + i];
+  }
+  gi += __shfl_xor_sync(0xffffffffu, gi, 1);
+  gi += __shfl_xor_sync(0xffffffffu, gi, 2);
+  if (i >= NPARAM || q != 0) return;
   const float t = (float)max(*step, 1u);
   const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
-  float gi = 0.0f;  // the CTAs' partial gradients, summed in slot order
-  for (uint32_t c = 0; c < nparts; ++c) gi += part[(size_t)c * NPARAM + i];
   if (!isfinite(gi)) {
     atomicOr(status, ST_GUIDE_NONFINITE);
     return;
@@ -190,6 +198,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   uint8_t* dzt = smem + TRAIN_OFF_DZ;
   uint8_t* at = smem + TRAIN_OFF_AT;
   __shared__ uint64_t mbar;
+  __shared__ uint64_t mbar_w;  // the packed weights' bulk copy
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   __shared__ float s_db[4 * 64 + 40];
@@ -208,13 +217,19 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   }
   if (tid == 0) {
     tc::mbar_init(&mbar, 1);
+    tc::mbar_init(&mbar_w, 1);
+    tc::fence_mbar_init();
+    tc::bulk_load(w, pack, PACK_BYTES, &mbar_w);  // weights by TMA while the rest is set up
     failed = 0;
     s_loss = 0.0f;
   }
   for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
-  for (int c = tid; c < PACK_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
   for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
+  if (tid == 0 && !tc::mbar_wait(&mbar_w, 0)) {
+    atomicOr(status, ST_GUIDE_NONFINITE << 1);
+    failed = 1;
+  }
   tc::fence_smem_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -383,6 +398,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   __syncthreads();
   for (int k = tid; k < 4 * 64 + 40; k += 128) slot[P_B + k] = ok ? s_db[k] : 0.0f;
   if (tid == 0) loss_part[blockIdx.x] = ok ? s_loss : 0.0f;
+  if (tid == 0 && failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy: bounded second chance
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -528,7 +544,7 @@ Status guide_launch_reduce(GuideNet& g, cudaStream_t s) {
 }
 
 Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
-  k_guide_adam<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grad_part, g.loss_part, g.nparts,
+  k_guide_adam<<<(4 * NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grad_part, g.loss_part, g.nparts,
                                                     g.loss_last, lr, g.d_step, g.status, g.w_bf16);
   LISA_CUDA(cudaGetLastError());
   return Status();

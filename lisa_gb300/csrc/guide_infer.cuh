@@ -142,6 +142,7 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   uint8_t* w = smem;
   uint8_t* act[2] = {smem + FWD_BYTES, smem + FWD_BYTES + 16384};
   __shared__ uint64_t mbar[2];
+  __shared__ uint64_t mbar_w;  // the packed weights' bulk copy
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   __shared__ __align__(16) float s_bias[4 * 64 + 48];
@@ -153,11 +154,17 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   if (tid == 0) {
     tc::mbar_init(&mbar[0], 1);
     tc::mbar_init(&mbar[1], 1);
+    tc::mbar_init(&mbar_w, 1);
+    tc::fence_mbar_init();
+    tc::bulk_load(w, pack, FWD_BYTES, &mbar_w);  // weights by TMA while the rest is set up
     failed = 0;
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
-  for (int c = tid; c < FWD_BYTES / 16; c += 128) ((uint4*)w)[c] = __ldg((const uint4*)pack + c);
   for (int k = tid; k < 4 * 64 + 48; k += 128) s_bias[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
+  if (tid == 0 && !tc::mbar_wait(&mbar_w, 0)) {
+    atomicOr(status, ST_GUIDE_NONFINITE << 1);
+    failed = 1;
+  }
   tc::fence_smem_async();
   tc::fence_before_sync();
   __syncthreads();
@@ -246,9 +253,11 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   }
   // after a time-out, give MMAs still in flight a bounded chance to finish
   // before their TMEM is freed
-  if (tid == 0)
+  if (tid == 0) {
     for (int k = 0; k < 2; ++k)
       if (busy[k]) tc::mbar_wait(&mbar[k], phase[k], 1u << 20);
+    if (failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();

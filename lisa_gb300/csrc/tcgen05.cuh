@@ -119,6 +119,37 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Bulk copy (TMA, untiled) of `bytes` from global to shared memory,
+// completing on `mbar` (transaction count).  Both addresses 16-byte aligned,
+// bytes a multiple of 16.  Issued by one thread after mbar_expect_tx.
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(smem_dst)),
+               "l"(gmem_src), "r"(bytes), "r"(smem_u32(mbar))
+               : "memory");
+}
+
+// Arrive once on mbar and add `bytes` to its expected transaction count.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+
+// Makes an mbarrier's initialisation visible to the async proxy (TMA).
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Copies `bytes` (a multiple of 16) from global to shared memory with bulk
+// copies of at most 16 KB, all completing on `mbar`, issued by the calling
+// thread; the caller waits for phase 0 of mbar (initialised with count 1).
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, uint32_t bytes, uint64_t* mbar) {
+  mbar_expect_tx(mbar, bytes);
+  for (uint32_t off = 0; off < bytes; off += 16384u) {
+    const uint32_t n = bytes - off < 16384u ? bytes - off : 16384u;
+    bulk_g2s((uint8_t*)smem_dst + off, (const uint8_t*)gmem_src + off, n, mbar);
+  }
+}
+
 // CH x 16 consecutive FP32 columns of this thread's TMEM lane: all loads
 // issued, then one wait.
 template <int CH>
