@@ -613,7 +613,10 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
           if (lit) {
             const DevMaterial& em = sc->mats[em_m];
             const float fcos = fmul(r, fdiv(cos_x, PI_F));
-            const float wl = fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(fcos, fcos)));
+            // power heuristic against the bounce, which the last vertex does not trace
+            const float wl = depth + 1 < (int)sc->num_bounces
+                                 ? fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(fcos, fcos)))
+                                 : 1.0f;
             const float4 c = b.ps_col[slot];
             const V3 col =
                 ld3(c) + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
@@ -734,7 +737,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
     const DevMaterial& em = sc.mats[__float_as_int(l1.y)];
     const float fcos = fmul(r, fdiv(cos_x, PI_F));
     const float pb = r * (c * (cos_x / PI_F) + (1.0f - c) * guide::mix_pdf(L, l0.x, l0.y, l0.z));
-    const float wl = (pl * pl) / (pl * pl + pb * pb);
+    const float wl = depth + 1 < (int)sc.num_bounces ? (pl * pl) / (pl * pl + pb * pb) : 1.0f;
     col = col + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
   }
   float prev = 0.0f;
@@ -1219,7 +1222,9 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       }));
       // the guide draws the bounces of the first guide_max_depth vertices
       // of a path (0 = all); deeper ones sample the BSDF
-      const bool guided_d = guided && (r.opts.guide_max_depth == 0 || d < r.opts.guide_max_depth);
+      // (and never the last one, whose bounce is not traced)
+      const bool guided_d = guided && d + 1 < waves[wv].bounces &&
+                            (r.opts.guide_max_depth == 0 || d < r.opts.guide_max_depth);
       LISA_TRY(stage(2, [&] {
         const dim3 g(physical ? r.nee_pb_blocks : r.nee_blocks), t(r.nee_threads);
         if (physical) {

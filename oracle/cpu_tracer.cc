@@ -633,7 +633,8 @@ V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters
           const V3 le_y = v3(c.emission[3 * em_m], c.emission[3 * em_m + 1], c.emission[3 * em_m + 2]);
           const float pl = (rec[3] * d2) / cos_y;
           const float fcos = r * (cos_x / PI_F);
-          const float wl = (pl * pl) / ((pl * pl) + (fcos * fcos));
+          // the last vertex's bounce is not traced: its emitter sample takes full weight
+          const float wl = i + 1 < bounces ? (pl * pl) / ((pl * pl) + (fcos * fcos)) : 1.0f;
           color = color + ((att * le_y) * (fcos / pl)) * wl;
         }
       }

@@ -16,7 +16,7 @@ def _quad(p0, p1, p2, p3, n):
     return v, nn
 
 
-def _scene(oracle, roughness, spp, seed=1):
+def _scene(oracle, roughness, spp, seed=1, bounces=2):
     floor_v, floor_n = _quad((-5, 0, -5), (-5, 0, 5), (5, 0, 5), (5, 0, -5), (0, 1, 0))
     cx, h, s = 0.3, 1.0, 0.2
     light_v, light_n = _quad((cx - s / 2, h, -s / 2), (cx + s / 2, h, -s / 2), (cx + s / 2, h, s / 2),
@@ -28,7 +28,7 @@ def _scene(oracle, roughness, spp, seed=1):
     mats = np.array([[roughness, 1.0, 1.0, 0.6, 0.5, 0.4, 0, 0, 0, 0],
                      [1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1, 5.0, 4.0, 3.0]], np.float32)
     sc = oracle.Scene(v, n, mi, mats, width=1, height=1, eye=(0.0, 0.5, 0.5), look_at=(0.0, 0.0, 0.0),
-                      fov=0.0005, spp=spp, bounces=2, seed=seed, estimator=1)
+                      fov=0.0005, spp=spp, bounces=bounces, seed=seed, estimator=1)
     return sc, (cx, h, s)
 
 
@@ -39,10 +39,13 @@ def _irradiance(cx, h, s, m=2000):
     return float(np.sum(h * h / d2 ** 2) * (s / m) ** 2)  # cos_x cos_y / d^2 = h^2 / d^4
 
 
-@pytest.mark.parametrize("roughness", [1.0, 0.5])
-def test_direct_lighting_matches_the_integral(oracle, roughness):
+@pytest.mark.parametrize("roughness,bounces", [(1.0, 2), (0.5, 2), (1.0, 1)])
+def test_direct_lighting_matches_the_integral(oracle, roughness, bounces):
+    """Two traces: emitter sampling and the traced bounce share the direct
+    light by MIS.  One trace: the floor is the last vertex, its bounce is not
+    traced, so the emitter sample carries it alone."""
     spp = 40000
-    sc, (cx, h, s) = _scene(oracle, roughness, spp)
+    sc, (cx, h, s) = _scene(oracle, roughness, spp, bounces=bounces)
     total, sq, rays = sc.render(use_bvh=True)
     mean = total[0] / spp
     var = np.maximum(sq[0] / spp - mean ** 2, 0.0)
