@@ -1,7 +1,7 @@
 // lisa: command-line renderer with the reference's interface
 // (src/LiSA/src/main.cc:6-27, src/LiSA/include/parse_args.hh:3-16):
 //
-//   lisa -s scene.rto [-d] [--guided] [--seed N] [--reference-rng]
+//   lisa -s scene.rto [-d] [--guided] [--physical] [--seed N] [--reference-rng]
 //
 // -s   scene file (required)
 // -d   the reference's interactive display mode, headless: progressive
@@ -43,6 +43,7 @@ int main(int argc, char** argv) {
   lisa_options opts;
   lisa_options_default(&opts);
   if (has_option(argc, argv, "--guided")) opts.mode = LISA_MODE_GUIDED;
+  if (has_option(argc, argv, "--physical")) opts.estimator = LISA_ESTIMATOR_PHYSICAL;
   if (has_option(argc, argv, "--reference-rng")) opts.rng = LISA_RNG_PER_PIXEL;
   if (const char* s = get_option(argc, argv, "--seed")) opts.seed = (uint32_t)std::strtoul(s, nullptr, 10);
   lisa_renderer* r = nullptr;
