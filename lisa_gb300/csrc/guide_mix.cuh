@@ -65,6 +65,7 @@ struct Lobe {
   float kappa;
   float w;           // mixture weight
   float norm;        // |raw mu|
+  float nk;          // vMF normalisation kappa / (2 pi (1 - e^{-2 kappa}))
 };
 
 // Decodes the 40 raw outputs: per lobe (mu xyz, kappa, logit).
@@ -89,18 +90,18 @@ __device__ __forceinline__ void decode(const float* o, Lobe* L) {
     L[k].my = ay * in;
     L[k].mz = az * in;
     L[k].norm = n;
-    L[k].kappa = __expf(fminf(fmaxf(o[5 * k + 3], KAPPA_LO), KAPPA_HI));
+    const float kap = __expf(fminf(fmaxf(o[5 * k + 3], KAPPA_LO), KAPPA_HI));
+    L[k].kappa = kap;
+    // 1 - e^{-2k} = -expm1(-2k); once per lobe, not per evaluation
+    L[k].nk = kap / (6.28318530717958647692f * -expm1f(-2.0f * kap));
     L[k].w *= iz;
   }
 }
 
 // vMF density at unit w.
 __device__ __forceinline__ float vmf_pdf(const Lobe& l, float wx, float wy, float wz) {
-  const float k = l.kappa;
   const float c = l.mx * wx + l.my * wy + l.mz * wz;
-  // k / (2 pi (1 - e^{-2k})) with 1 - e^{-2k} = -expm1(-2k)
-  const float norm = k / (6.28318530717958647692f * -expm1f(-2.0f * k));
-  return norm * __expf(k * (c - 1.0f));
+  return l.nk * __expf(l.kappa * (c - 1.0f));
 }
 
 __device__ __forceinline__ float mix_pdf(const Lobe* L, float wx, float wy, float wz) {
