@@ -281,13 +281,17 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
           }
           const V3 c = ld3(col) + le;
           b.ps_col[slot] = make_float4(c.x, c.y, c.z, col.w);
-        } else {
+        } else if (!PHYS || depth < (int)sc.num_bounces) {
+          // (physically based: the ray leaving the last vertex only gathers
+          // the emission it reaches, so any other hit ends the path)
           const float4 d4 = b.rd[q][i];
           d = ld3(d4);
           const float t = __int_as_float(h.y);
           p = ld3(o4) + t * d;
           N = barycentric_normal(p, sc.prims + 5ull * h.x);
-          const bool last = depth + 1 >= (int)sc.num_bounces;
+          // the reference estimator traces num_bounces rays; the physically
+          // based one also the ray leaving its last vertex
+          const bool last = !PHYS && depth + 1 >= (int)sc.num_bounces;
           if (m.cls == MAT_DIELECTRIC) {
             float cosI = dot(d, N);
             float eta;
@@ -613,10 +617,9 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
           if (lit) {
             const DevMaterial& em = sc->mats[em_m];
             const float fcos = fmul(r, fdiv(cos_x, PI_F));
-            // power heuristic against the bounce, which the last vertex does not trace
-            const float wl = depth + 1 < (int)sc->num_bounces
-                                 ? fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(fcos, fcos)))
-                                 : 1.0f;
+            // power heuristic against the bounce (traced at every vertex, the
+            // last one's for the emission it reaches only)
+            const float wl = fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(fcos, fcos)));
             const float4 c = b.ps_col[slot];
             const V3 col =
                 ld3(c) + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
@@ -629,7 +632,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
           } else {
             nd = reflect(ld3(b.nee_c[entry]), Ns);
           }
-          want_ray = depth + 1 < (int)sc->num_bounces && !is_zero(nd);
+          want_ray = !is_zero(nd);
           b.ps_rng[slot] = seed;
           b.ps_att[slot] = make_float4(att.x, att.y, att.z, prev);
         }
@@ -737,7 +740,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
     const DevMaterial& em = sc.mats[__float_as_int(l1.y)];
     const float fcos = fmul(r, fdiv(cos_x, PI_F));
     const float pb = r * (c * (cos_x / PI_F) + (1.0f - c) * guide::mix_pdf(L, l0.x, l0.y, l0.z));
-    const float wl = depth + 1 < (int)sc.num_bounces ? (pl * pl) / (pl * pl + pb * pb) : 1.0f;
+    const float wl = (pl * pl) / (pl * pl + pb * pb);
     col = col + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
   }
   float prev = 0.0f;
@@ -755,14 +758,14 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
     const float weight = (pc > 0.0f && qm > 0.0f && isfinite(qm)) ? pc / qm : 0.0f;
     att = att * weight;
     prev = r * qm;
-    want = depth + 1 < (int)sc.num_bounces && weight > 0.0f;
+    want = weight > 0.0f;
     const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
     keep_record(b, depth, slot, 0.0f, make_float4(p.x, p.y, p.z, weight), make_float4(N.x, N.y, N.z, nd.x),
                 make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y), make_float4(att.x, att.y, att.z, nd.z), col);
     ++guided_n;
   } else {
     nd = reflect(D, Ns);
-    want = depth + 1 < (int)sc.num_bounces;
+    want = true;
   }
   b.ps_col[slot] = make_float4(col.x, col.y, col.z, cw.w);
   b.ps_rng[slot] = seed;
@@ -1209,7 +1212,10 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       k_raygen<<<r.sm_count * 8, 256, 0, r.stream>>>(b, wd);
       return Status();
     }));
-    for (uint32_t d = 0; d < waves[wv].bounces; ++d) {
+    // the physically based estimator traces one more ray per path, the one
+    // leaving its last vertex, for the emission it reaches (no vertex)
+    const uint32_t depths = waves[wv].bounces + (physical ? 1u : 0u);
+    for (uint32_t d = 0; d < depths; ++d) {
       LISA_TRY(stage(0, [&] {
         if (counting) k_trace<true><<<r.trace_blocks, r.trace_threads, 0, r.stream>>>(b, (int)d);
         else k_trace<false><<<r.trace_blocks, r.trace_threads, 0, r.stream>>>(b, (int)d);
@@ -1220,10 +1226,11 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
         else k_shade<false><<<r.shade_blocks, r.shade_threads, 0, r.stream>>>(b, (int)d);
         return Status();
       }));
+      if (d == waves[wv].bounces) break;  // the emission-only depth has no vertices
       // the guide draws the bounces of the first guide_max_depth vertices
-      // of a path (0 = all); deeper ones sample the BSDF
-      // (and never the last one, whose bounce is not traced)
-      const bool guided_d = guided && d + 1 < waves[wv].bounces &&
+      // of a path (0 = all); deeper ones sample the BSDF (and, with the
+      // reference estimator, never the last one, whose bounce is not traced)
+      const bool guided_d = guided && (physical || d + 1 < waves[wv].bounces) &&
                             (r.opts.guide_max_depth == 0 || d < r.opts.guide_max_depth);
       LISA_TRY(stage(2, [&] {
         const dim3 g(physical ? r.nee_pb_blocks : r.nee_blocks), t(r.nee_threads);
@@ -1359,7 +1366,7 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
     if (key != r.graph_key || !r.graph_exec) {
       if (tm.on) {  // create the timing events before capture begins
         size_t need = 0;
-        for (const WaveLaunch& w : wb) need += 2ull * (5ull * w.bounces + 6 + 2ull * w.steps);
+        for (const WaveLaunch& w : wb) need += 2ull * (5ull * (w.bounces + 1) + 6 + 2ull * w.steps);
         while (r.ev_pool.size() < need) {
           cudaEvent_t e;
           LISA_CUDA(cudaEventCreate(&e));

@@ -25,7 +25,10 @@
 // luminance with two-sided emitters, cosine-weighted diffuse sampling,
 // power-heuristic MIS between the two, roughness as the weight of the
 // diffuse lobe against a mirror, and Schlick's Fresnel term evaluated on the
-// less dense side (the transmitted cosine when leaving a medium).
+// less dense side (the transmitted cosine when leaving a medium).  A path
+// has at most `bounces` scattering vertices; the ray leaving the last one is
+// still traced for the emission it reaches (the BSDF half of that vertex's
+// MIS), so every emitter sample keeps its power-heuristic weight.
 //
 // Deliberate readings of the reference (shared with the product):
 //   * a zero direction (total internal reflection) is a miss, not traced;
@@ -385,6 +388,7 @@ V3 trace_path(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters& c
       color = color + v3(c.emission[3 * m], c.emission[3 * m + 1], c.emission[3 * m + 2]) * att;
       break;
     }
+    if (i == bounces) break;
     const V3 p = o + t * d;
     const float* tv = c.v + 9ull * prim;
     const float* tn = c.n + 9ull * prim;
@@ -549,7 +553,10 @@ V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters
   V3 color = v3(0.0f, 0.0f, 0.0f), att = v3(1.0f, 1.0f, 1.0f);
   float prev_pdf = 0.0f;  // solid-angle pdf of the last diffuse bounce; 0 after camera / specular
   const Emitters& em = c.em;
-  for (int i = 0; i < bounces; ++i) {
+  // `bounces` scattering vertices; the ray leaving the last one is traced
+  // for the emission it reaches only (its MIS half of that vertex's
+  // emitter sample), with no vertex of its own
+  for (int i = 0; i <= bounces; ++i) {
     if (is_zero(d)) break;
     if (i == 0) ++cnt.primary; else ++cnt.bounce;
     int prim;
@@ -572,6 +579,7 @@ V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters
       }
       break;
     }
+    if (i == bounces) break;
     const V3 p = o + t * d;
     const float* tv = c.v + 9ull * prim;
     const float* tn = c.n + 9ull * prim;
@@ -633,8 +641,7 @@ V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters
           const V3 le_y = v3(c.emission[3 * em_m], c.emission[3 * em_m + 1], c.emission[3 * em_m + 2]);
           const float pl = (rec[3] * d2) / cos_y;
           const float fcos = r * (cos_x / PI_F);
-          // the last vertex's bounce is not traced: its emitter sample takes full weight
-          const float wl = i + 1 < bounces ? (pl * pl) / ((pl * pl) + (fcos * fcos)) : 1.0f;
+          const float wl = (pl * pl) / ((pl * pl) + (fcos * fcos));
           color = color + ((att * le_y) * (fcos / pl)) * wl;
         }
       }

@@ -55,7 +55,7 @@ def test_path_by_path_icosphere(gpu, oracle):
     assert abs(int(st.rays_shadow) - int(rays[2])) <= 0.002 * rays[2]
 
 
-def _floor_and_light(roughness, spp):
+def _floor_and_light(roughness, spp, bounces=2):
     """Diffuse floor (albedo 0.6, 0.5, 0.4) and a 0.2 x 0.2 emitter
     (5, 4, 3) one unit above, centred 0.3 to the side; one pixel looking at
     the origin."""
@@ -68,14 +68,17 @@ def _floor_and_light(roughness, spp):
                      [1.0, 1.0, 1.0, 1.0, 1.0, 1.0, 1, 5.0, 4.0, 3.0]], np.float32)
     return L.params_from_arrays(np.concatenate([fv, lv]), np.concatenate([fn, ln]),
                                 np.array([0, 0, 1, 1], np.int32), mats, 1, 1, (0.0, 0.5, 0.5), (0.0, 0.0, 0.0),
-                                0.0005, spp, 2)
+                                0.0005, spp, bounces)
 
 
-@pytest.mark.parametrize("roughness", [1.0, 0.5])
-def test_direct_lighting_matches_the_integral(gpu, roughness):
+@pytest.mark.parametrize("roughness,bounces", [(1.0, 2), (0.5, 2), (1.0, 1)])
+def test_direct_lighting_matches_the_integral(gpu, roughness, bounces):
+    """With one bounce the floor is the last vertex; the ray leaving it is
+    traced for emission only, so MIS still splits the direct light."""
     spp = 1 << 20
-    r = L.Renderer(_floor_and_light(roughness, spp), estimator=PHYS)
-    r.render()
+    r = L.Renderer(_floor_and_light(roughness, spp, bounces), estimator=PHYS)
+    st = r.render()
+    assert st.rays_bounce > 0
     mean, var = r.image(variance=True)
     u = (np.arange(2000) + 0.5) / 2000 * 0.2 - 0.1
     U, V = np.meshgrid(u, u, indexing="ij")

@@ -102,13 +102,17 @@ def test_ppm_payload_and_file(gpu, oracle, tmp_path):
     assert data.startswith(hdr) and data[len(hdr):] == payload.tobytes()
 
 
-def test_batch_of_uneven_scenes_matches_single_renders(gpu):
+@pytest.mark.parametrize("estimator", [0, 1])
+def test_batch_of_uneven_scenes_matches_single_renders(gpu, estimator):
+    """Scenes with different bounce counts share waves; with the physically
+    based estimator each path's emission-only last ray falls at its own
+    scene's depth."""
     a = scenes.cornell_box(width=24, height=16, num_samples=2, num_bounces=3)
     b = scenes.icosphere_box(level=3, width=20, height=20, num_samples=3, num_bounces=5)
-    batch = L.Renderer([L.params_from_scene(a), L.params_from_scene(b)], paths_in_flight=700)
+    batch = L.Renderer([L.params_from_scene(a), L.params_from_scene(b)], paths_in_flight=700, estimator=estimator)
     batch.render()
     for k, sc in enumerate((a, b)):
-        single = L.Renderer(L.params_from_scene(sc))
+        single = L.Renderer(L.params_from_scene(sc), estimator=estimator)
         single.render()
         assert np.array_equal(batch.image(k), single.image()), k
 

@@ -41,9 +41,10 @@ def _irradiance(cx, h, s, m=2000):
 
 @pytest.mark.parametrize("roughness,bounces", [(1.0, 2), (0.5, 2), (1.0, 1)])
 def test_direct_lighting_matches_the_integral(oracle, roughness, bounces):
-    """Two traces: emitter sampling and the traced bounce share the direct
-    light by MIS.  One trace: the floor is the last vertex, its bounce is not
-    traced, so the emitter sample carries it alone."""
+    """Emitter sampling and the traced bounce share the direct light by
+    MIS.  With one bounce the floor is the last vertex: the ray leaving it is
+    still traced, for the emission it reaches only, so the two weights still
+    sum to one."""
     spp = 40000
     sc, (cx, h, s) = _scene(oracle, roughness, spp, bounces=bounces)
     total, sq, rays = sc.render(use_bvh=True)
@@ -53,7 +54,7 @@ def test_direct_lighting_matches_the_integral(oracle, roughness, bounces):
     expect = roughness * np.array([0.6, 0.5, 0.4]) / np.pi * E * np.array([5.0, 4.0, 3.0])
     sigma = np.sqrt(var / spp)
     assert np.all(np.abs(mean - expect) < 4 * sigma + 1e-6), (mean, expect, sigma)
-    assert rays[0] == spp and rays[2] > 0
+    assert rays[0] == spp and rays[1] > 0 and rays[2] > 0  # the floor's bounce is traced
 
 
 def test_independent_streams_agree(oracle):
