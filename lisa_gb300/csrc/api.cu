@@ -232,6 +232,16 @@ Status build_emitters(Renderer& r, const lisa_renderer_params& p, SceneGpu& s, s
   return Status();
 }
 
+// Per triangle: its material if that is an emitter, else -1 (what the BVH
+// leaves carry, so the emitter search reads the class of a hit without a
+// material look-up).
+__global__ void k_emit_of_prim(int32_t* m, uint32_t n, const int32_t* em, uint32_t nm) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t k = (uint32_t)m[i];
+    m[i] = k < nm ? em[k] : -1;
+  }
+}
+
 Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   LISA_TRY(validate(p));
   s.params = p;
@@ -257,6 +267,19 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
     LISA_TRY(r.arena.alloc((void**)&s.prims, sizeof(float4) * 5ull * T, "triangle records"));
     k_pack_prims<<<r.sm_count * 8, 256, 0, r.stream>>>(d_v, d_n, d_m, T, s.prims);
     cudaError_t e = cudaGetLastError();
+    // then d_m becomes what the BVH leaves carry: the emitter material or -1
+    std::vector<int32_t> em(std::max(p.num_materials, 1), -1);
+    for (int i = 0; i < p.num_materials; ++i) em[i] = p.materials[i].emit ? i : -1;
+    int32_t* d_em = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&d_em, sizeof(int32_t) * em.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_em, em.data(), sizeof(int32_t) * em.size(), cudaMemcpyHostToDevice, r.stream);
+    if (e == cudaSuccess) {
+      k_emit_of_prim<<<r.sm_count * 8, 256, 0, r.stream>>>(d_m, T, d_em, (uint32_t)em.size());
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);
+    if (d_em) cudaFree(d_em);
     if (e != cudaSuccess) {
       cudaFree(d_v);
       cudaFree(d_n);

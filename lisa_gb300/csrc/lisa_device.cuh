@@ -13,7 +13,8 @@
 //            meta[i] = count<<5 | offset (count 1..3 triangles at
 //            tri_base + offset); meta 0 and imask 0 = empty slot.
 //   tris   : 3 x float4 per leaf triangle slot, in leaf order:
-//            (v0.xyz, original triangle id as int bits), (v1, material), (v2, 0)
+//            (v0.xyz, original triangle id as int bits),
+//            (v1, its material if that is an emitter, else -1), (v2, 0)
 //   prims  : 5 x float4 per original triangle (shading record):
 //            (v0, n0.x) (v1, n0.y) (v2, n0.z) (n1, n2.x) (n2.y, n2.z, mat, 0)
 //   mats   : DevMaterial, 48 B each
@@ -247,7 +248,7 @@ struct TravState {
   float best_t;
   float cull;  // best_t * (1+2^-16) + slack
   int best_prim;
-  int best_mat;  // material of the best hit (carried by the leaf triangle)
+  int best_mat;  // emitter material of the best hit, -1 if not an emitter (from the leaf triangle)
   uint32_t node;
   int sp;
 };
@@ -268,11 +269,21 @@ __device__ __forceinline__ bool trav_begin(TravState& s, const TraceScene& sc, V
   return true;
 }
 
-// Processes one node.  Returns true when the traversal is finished
-// (s.best_prim / s.best_t hold the result, best_prim -1 on a miss).
+// One node of the traversal, in three parts.  trav_node tests the node's
+// eight child boxes, pushes the internal children it hits (with their entry
+// distances) and returns, as a bitmask over the node's triangle slots, the
+// triangles of the leaf children it hits.  The triangles are then tested,
+// by the lane itself (trav_tris) or by its warp (trav_tris_warp), and
+// trav_pop orders the pushed children and moves to the next node.
+struct NodeWork {
+  uint32_t tmask;     // triangle slots tri_base + bit index still to test
+  uint32_t tri_base;
+  int sp0;            // stack depth before this node's pushes
+};
+
 template <bool COUNT>
-__device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, uint2* stack, uint32_t& visits,
-                                          uint32_t& tests, uint32_t* status) {
+__device__ __forceinline__ NodeWork trav_node(TravState& s, const TraceScene& sc, uint2* stack, uint32_t& visits,
+                                              uint32_t* status) {
   const RayPre& r = s.r;
   if (COUNT) ++visits;
   const uint4* np = sc.nodes + 5ull * s.node;
@@ -301,12 +312,14 @@ __device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, ui
   const uint32_t nz0 = negz ? n4.z : n3.x, nz1 = negz ? n4.w : n3.y;
   const uint32_t fz0 = negz ? n3.x : n4.z, fz1 = negz ? n3.y : n4.w;
   const uint32_t imask = n0.w >> 24;
-  const uint32_t child_base = n1.x, tri_base = n1.y;
+  const uint32_t child_base = n1.x;
+  NodeWork w;
+  w.tri_base = n1.y;
   // child boxes: hit mask; internal children that are hit go straight onto
   // the stack with their entry distance (predicated stores, no branches)
   uint32_t hit = 0;
-  const int sp0 = s.sp;
-  int sp = sp0;
+  w.sp0 = s.sp;
+  int sp = w.sp0;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
     const int b = c & 3;
@@ -325,37 +338,153 @@ __device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, ui
       stack[sp++] = make_uint2(child_base + meta, __float_as_uint(tn));
     }
   }
-  if (status && (imask & hit) && sp == TRAV_STACK && __popc(imask & hit) > sp - sp0) atomicOr(status, ST_STACK_OVERFLOW);
+  if (status && (imask & hit) && sp == TRAV_STACK && __popc(imask & hit) > sp - w.sp0)
+    atomicOr(status, ST_STACK_OVERFLOW);
+  s.sp = sp;
   // occupied slots: internal children and leaves with a non-zero meta byte
   uint32_t leafmask = 0;
 #pragma unroll
   for (int c = 0; c < 8; ++c) leafmask |= ((((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xe0u) ? 1u : 0u) << c;
   leafmask &= ~imask & hit;
   // triangles of the hit leaves, as a bitmask over the node's triangle slots
-  uint32_t tmask = 0;
+  w.tmask = 0;
   while (leafmask) {
     const int c = __ffs(leafmask) - 1;
     leafmask &= leafmask - 1;
     const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xffu;
-    tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+    w.tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
   }
-  while (tmask) {
-    const int j = __ffs(tmask) - 1;
-    tmask &= tmask - 1;
-    const float4* tp = sc.tris + 3ull * (tri_base + (uint32_t)j);
+  return w;
+}
+
+// Keeps the hit (t, prim) if it is nearer, or as near with a lower
+// triangle index (the brute-force tie rule).
+__device__ __forceinline__ void trav_take(TravState& s, float t, int prim, int mat) {
+  if (t < s.best_t || (t == s.best_t && prim < s.best_prim)) {
+    s.best_t = t;
+    s.best_prim = prim;
+    s.best_mat = mat;
+    s.cull = fmaf(t, 1.52587890625e-5f, t) + s.r.slack;
+  }
+}
+
+// The lane tests its own triangles.
+template <bool COUNT>
+__device__ __forceinline__ void trav_tris(TravState& s, const TraceScene& sc, NodeWork w, uint32_t& tests) {
+  while (w.tmask) {
+    const int j = __ffs(w.tmask) - 1;
+    w.tmask &= w.tmask - 1;
+    const float4* tp = sc.tris + 3ull * (w.tri_base + (uint32_t)j);
     const float4 a = __ldg(tp + 0), bb = __ldg(tp + 1), cc = __ldg(tp + 2);
     if (COUNT) ++tests;
-    const float t = intersect_tri(r, a, bb, cc, s.tmin);
-    const int prim = __float_as_int(a.w);
-    if (t < s.best_t || (t == s.best_t && prim < s.best_prim)) {
-      s.best_t = t;
-      s.best_prim = prim;
-      s.best_mat = __float_as_int(bb.w);
-      s.cull = fmaf(t, 1.52587890625e-5f, t) + r.slack;
-    }
+    trav_take(s, intersect_tri(s.r, a, bb, cc, s.tmin), __float_as_int(a.w), __float_as_int(bb.w));
   }
-  // order the children just pushed by entry distance, nearest on top
+}
+
+// Per-warp scratch of trav_tris_warp (shared memory).
+struct TriPass {
+  unsigned long long key[32];  // (t bits << 32 | triangle id) of each lane's best hit
+  int mat[32];
+  int owner[32];               // lane whose triangles start at this position of a pass
+};
+
+// The warp tests the triangles of all its lanes together, 32 at a time:
+// the lanes' triangle lists are laid end to end (a prefix sum of their
+// counts) and lane j of a pass takes the j-th triangle of the pass, with
+// the owner's ray.  The owner's best hit is the minimum of the 64-bit keys
+// (t, triangle id) -- t is positive, so its bits order as the float -- the
+// same choice as the lane's own loop with its tie rule.  Called by all 32
+// lanes; lanes without a ray pass w.tmask = 0.
+template <bool COUNT>
+__device__ __forceinline__ void trav_tris_warp(TravState& s, const TraceScene& sc, NodeWork w, uint32_t& tests,
+                                               TriPass& tp) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t cnt = __popc(w.tmask);
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0) return;
+  // when no lane has more triangles than the passes a warp would need,
+  // the lanes' own loops are cheaper than the exchange
+  if (__reduce_max_sync(0xffffffffu, cnt) <= ((total + 31u) >> 5)) {
+    if (cnt) trav_tris<COUNT>(s, sc, w, tests);
+    return;
+  }
+  const uint32_t excl = incl - cnt;
+  const unsigned long long key0 =
+      ((unsigned long long)__float_as_uint(s.best_t) << 32) | (uint32_t)s.best_prim;
+  tp.key[lane] = key0;
+  for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+    // positions of this pass where a lane's list starts (the list holding
+    // position 0 starts there too)
+    const bool here = cnt && excl < k0 + 32 && excl + cnt > k0;
+    const uint32_t pos = excl > k0 ? excl - k0 : 0u;
+    if (here) tp.owner[pos] = lane;
+    const uint32_t starts = __reduce_or_sync(0xffffffffu, here ? 1u << pos : 0u);
+    __syncwarp();
+    const uint32_t k = k0 + (uint32_t)lane;
+    // the list holding position `lane`: the last start at or below it
+    const int first = 31 - __clz(starts & (0xffffffffu >> (31 - lane)));
+    const int o = tp.owner[first];
+    const uint32_t o_excl = __shfl_sync(0xffffffffu, excl, o);
+    uint32_t m = __shfl_sync(0xffffffffu, w.tmask, o);
+    const uint32_t o_base = __shfl_sync(0xffffffffu, w.tri_base, o);
+    RayPre r;
+    r.ox = __shfl_sync(0xffffffffu, s.r.ox, o);
+    r.oy = __shfl_sync(0xffffffffu, s.r.oy, o);
+    r.oz = __shfl_sync(0xffffffffu, s.r.oz, o);
+    r.k = __shfl_sync(0xffffffffu, s.r.k, o);
+    r.Sx = __shfl_sync(0xffffffffu, s.r.Sx, o);
+    r.Sy = __shfl_sync(0xffffffffu, s.r.Sy, o);
+    r.Sz = __shfl_sync(0xffffffffu, s.r.Sz, o);
+    const float tmin = __shfl_sync(0xffffffffu, s.tmin, o);
+    const unsigned long long tris_p = __shfl_sync(0xffffffffu, (unsigned long long)sc.tris, o);
+    const unsigned long long okey = __shfl_sync(0xffffffffu, key0, o);
+    bool better = false;
+    unsigned long long key = 0;
+    int mat = 0;
+    if (k < total) {
+      // the (k - o_excl)-th remaining triangle of the owner's list
+      for (uint32_t i = k - o_excl; i > 0; --i) m &= m - 1;
+      const uint32_t j = (uint32_t)(__ffs(m) - 1);
+      const float4* tq = (const float4*)tris_p + 3ull * (o_base + j);
+      const float4 a = __ldg(tq + 0), bb = __ldg(tq + 1), cc = __ldg(tq + 2);
+      if (COUNT) ++tests;
+      const float t = intersect_tri(r, a, bb, cc, tmin);
+      const int prim = __float_as_int(a.w);
+      const float bt = __uint_as_float((uint32_t)(okey >> 32));
+      const int bp = (int)(uint32_t)okey;
+      if (t < bt || (t == bt && prim < bp)) {
+        better = true;
+        key = ((unsigned long long)__float_as_uint(t) << 32) | (uint32_t)prim;
+        mat = __float_as_int(bb.w);
+        atomicMin(&tp.key[o], key);
+      }
+    }
+    __syncwarp();
+    if (better && tp.key[o] == key) tp.mat[o] = mat;
+    __syncwarp();
+  }
+  const unsigned long long best = tp.key[lane];
+  if (best != key0) {
+    s.best_t = __uint_as_float((uint32_t)(best >> 32));
+    s.best_prim = (int)(uint32_t)best;
+    s.best_mat = tp.mat[lane];
+    s.cull = fmaf(s.best_t, 1.52587890625e-5f, s.best_t) + s.r.slack;
+  }
+  __syncwarp();
+}
+
+// Orders the children trav_node pushed by entry distance (nearest on top)
+// and moves to the nearest child not culled.  Returns true when the
+// traversal is finished.
+__device__ __forceinline__ bool trav_pop(TravState& s, uint2* stack, int sp0) {
   // (entry distances are positive, so their bit patterns order as floats)
+  const int sp = s.sp;
   for (int i = sp0 + 1; i < sp; ++i) {
     const uint2 e = stack[i];
     int k = i;
@@ -365,7 +494,6 @@ __device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, ui
     }
     stack[k] = e;
   }
-  s.sp = sp;
   while (s.sp > 0) {
     const uint2 e = stack[--s.sp];
     if (__uint_as_float(e.y) <= s.cull) {
@@ -374,6 +502,32 @@ __device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, ui
     }
   }
   return true;
+}
+
+// Processes one node with the lane's own triangle loop.  Returns true when
+// the traversal is finished (s.best_prim / s.best_t hold the result,
+// best_prim -1 on a miss).
+template <bool COUNT>
+__device__ __forceinline__ bool trav_step(TravState& s, const TraceScene& sc, uint2* stack, uint32_t& visits,
+                                          uint32_t& tests, uint32_t* status) {
+  const NodeWork w = trav_node<COUNT>(s, sc, stack, visits, status);
+  trav_tris<COUNT>(s, sc, w, tests);
+  return trav_pop(s, stack, w.sp0);
+}
+
+// The same step for a whole warp (all 32 lanes call it), the triangles
+// tested by trav_tris_warp.  Returns true for an active lane whose
+// traversal is finished; inactive lanes get false.
+template <bool COUNT>
+__device__ __forceinline__ bool trav_step_warp(bool active, TravState& s, const TraceScene& sc, uint2* stack,
+                                               uint32_t& visits, uint32_t& tests, uint32_t* status, TriPass& tp) {
+  NodeWork w;
+  w.tmask = 0;
+  w.tri_base = 0;
+  w.sp0 = 0;
+  if (active) w = trav_node<COUNT>(s, sc, stack, visits, status);
+  trav_tris_warp<COUNT>(s, sc, w, tests, tp);
+  return active && trav_pop(s, stack, w.sp0);
 }
 
 template <bool COUNT>

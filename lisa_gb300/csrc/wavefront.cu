@@ -195,6 +195,8 @@ __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
   TraceScene ts;
   uint32_t ray = 0, visits = 0, tests = 0;
   bool active = false, exhausted = false;
+  __shared__ TriPass tri_pass[4];
+  TriPass& tp = tri_pass[threadIdx.x >> 5];
   while (true) {
     // take new rays only once enough lanes are idle (see k_nee)
     if (__popc(__ballot_sync(FULL, active)) <= (int)b.refill_busy_max) {
@@ -220,7 +222,7 @@ __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
       }
       if (!__any_sync(FULL, active || !exhausted)) break;
     }
-    if (active && trav_step<COUNT>(s, ts, stack, visits, tests, &b.ctrl->status)) {
+    if (trav_step_warp<COUNT>(active, s, ts, stack, visits, tests, &b.ctrl->status, tp)) {
       b.hit[ray] = make_int2(s.best_prim, s.best_prim >= 0 ? __float_as_int(s.best_t) : 0x7f800000);
       active = false;
     }
@@ -401,6 +403,8 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
   s.r.ox = s.r.oy = s.r.oz = 0.0f;
   uint32_t shadow = 0, visits = 0, tests = 0;
   bool pending = false;  // a finished shadow ray not yet evaluated
+  __shared__ TriPass tri_pass[4];
+  TriPass& tp = tri_pass[threadIdx.x >> 5];
   while (true) {
     // Bookkeeping (evaluate finished rays, finish and fetch vertices, start
     // rays) runs only once enough lanes are idle, so its divergent code is
@@ -414,8 +418,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
         if (s.best_prim >= 0) {
           // the occlusion hit program marks a hit only on an emitter and
           // otherwise leaves the flag as it was (shader.cu:177-184)
-          const int hm = s.best_mat;
-          if (sc->mats[hm].cls == MAT_EMIT) stale = hm;
+          if (s.best_mat >= 0) stale = s.best_mat;
         } else {
           stale = -1;  // miss (shader.cu:172-175)
         }
@@ -487,7 +490,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
         pending = !ray_active;  // nothing to traverse: a miss
       }
     }
-    if (ray_active && trav_step<COUNT>(s, ts, stack, visits, tests, &b.ctrl->status)) {
+    if (trav_step_warp<COUNT>(ray_active, s, ts, stack, visits, tests, &b.ctrl->status, tp)) {
       ray_active = false;
       pending = true;
     }
@@ -597,6 +600,8 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
   float pl = 0.0f, cos_x = 0.0f;
   s.r.ox = s.r.oy = s.r.oz = 0.0f;
   uint32_t nshadow = 0, visits = 0, tests = 0;
+  __shared__ TriPass tri_pass[4];
+  TriPass& tp = tri_pass[threadIdx.x >> 5];
   while (true) {
     const uint32_t busy = __ballot_sync(FULL, ray_active);
     if (__popc(busy) <= (int)b.refill_busy_max) {
@@ -696,7 +701,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
       }
       if (!__any_sync(FULL, have)) break;
     }
-    if (ray_active && trav_step<COUNT>(s, ts, stack, visits, tests, &b.ctrl->status)) {
+    if (trav_step_warp<COUNT>(ray_active, s, ts, stack, visits, tests, &b.ctrl->status, tp)) {
       ray_active = false;
       pending = true;
     }
