@@ -41,7 +41,8 @@ __device__ __forceinline__ float dot(V3 a, V3 b) {
   return fadd(fadd(fmul(a.x, b.x), fmul(a.y, b.y)), fmul(a.z, b.z));
 }
 __device__ __forceinline__ V3 normalize(V3 v) {
-  const float inv = fdiv(1.0f, fsqrt(dot(v, v)));
+  // the correctly rounded reciprocal: the value of 1.0f / x
+  const float inv = __frcp_rn(fsqrt(dot(v, v)));
   return v * inv;
 }
 // i - (2*n)*dot(n,i)
@@ -72,8 +73,9 @@ __device__ __forceinline__ uint32_t lcg(uint32_t& prev) {
   prev = 1664525u * prev + 1013904223u;
   return prev & 0x00FFFFFFu;
 }
-// [0, 1): exact (24-bit integer times 2^-24)
-__device__ __forceinline__ float rnd(uint32_t& s) { return fdiv((float)lcg(s), 16777216.0f); }
+// [0, 1): exact (24-bit integer times 2^-24; the same value as the quotient
+// by 2^24 that the reference computes)
+__device__ __forceinline__ float rnd(uint32_t& s) { return fmul((float)lcg(s), 5.9604644775390625e-8f); }
 // [-1, 1): rnd*2 - 1
 __device__ __forceinline__ float rng11(uint32_t& s) { return fsub(fmul(rnd(s), 2.0f), 1.0f); }
 
