@@ -301,6 +301,32 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
               dz = s.bvh.bmax[2] - s.bvh.bmin[2];
   s.extent = std::sqrt(dx * dx + dy * dy + dz * dz);
   if (!(s.extent > 0.0f) || !std::isfinite(s.extent)) s.extent = 1.0f;
+  // bounds of the emissive triangles, padded by 1e-4 of the scene diagonal
+  // (far more than the triangle test's rounding outside an edge): an
+  // emitter-search ray that misses them cannot end on an emitter
+  {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool any = false;
+    for (uint32_t t = 0; t < T; ++t) {
+      const int32_t m = p.mat_indices[t];
+      if (m < 0 || m >= p.num_materials || !p.materials[m].emit) continue;
+      any = true;
+      for (int j = 0; j < 3; ++j) {
+        const lisa_float3& v = p.vertices[3ull * t + j];
+        const float c[3] = {v.x, v.y, v.z};
+        for (int k = 0; k < 3; ++k) {
+          lo[k] = std::min(lo[k], c[k]);
+          hi[k] = std::max(hi[k], c[k]);
+        }
+      }
+    }
+    s.has_emit_box = any;
+    const float pad = 1e-4f * s.extent;
+    for (int k = 0; k < 3; ++k) {
+      s.emit_lo[k] = any ? lo[k] - pad : 0.0f;
+      s.emit_hi[k] = any ? hi[k] + pad : 0.0f;
+    }
+  }
   // materials
   std::vector<DevMaterial> dm(std::max(p.num_materials, 1));
   for (int i = 0; i < p.num_materials; ++i) dm[i] = to_dev(p.materials[i]);
@@ -336,6 +362,11 @@ SceneDev scene_dev(const Renderer& r, const SceneGpu& s) {
   d.width = s.params.width;
   d.height = s.params.height;
   d.num_bounces = s.params.num_bounces;
+  d.has_emit_box = s.has_emit_box ? 1u : 0u;
+  for (int k = 0; k < 3; ++k) {
+    d.emit_lo[k] = s.emit_lo[k];
+    d.emit_hi[k] = s.emit_hi[k];
+  }
   for (int k = 0; k < 3; ++k) {
     d.eye[k] = s.eye[k];
     d.U[k] = s.U[k];

@@ -84,7 +84,8 @@ struct SceneDev {
   const float4* emit;
   const float* emit_cdf;
   uint32_t num_emit;
-  uint32_t pad2;
+  uint32_t has_emit_box;     // the scene has emissive triangles, all inside emit_lo..emit_hi
+  float emit_lo[3], emit_hi[3];
 };
 
 // One group of a wave: `nplanes` consecutive sample planes of pixels
@@ -251,13 +252,18 @@ struct TravState {
   int best_mat;  // emitter material of the best hit, -1 if not an emitter (from the leaf triangle)
   uint32_t node;
   int sp;
+  bool any;  // stop at the first hit found (only whether there is one matters)
 };
 
 __device__ __forceinline__ float byte_f(uint32_t w, int b) { return (float)((w >> (8 * b)) & 0xffu); }
 
 // Starts a ray; returns false when there is nothing to traverse (empty
-// scene or zero direction), in which case the ray is a miss.
-__device__ __forceinline__ bool trav_begin(TravState& s, const TraceScene& sc, V3 o, V3 d, float tmin, float tmax) {
+// scene or zero direction), in which case the ray is a miss.  With `any`
+// the traversal ends at the first hit it finds: best_prim then says only
+// whether the segment (tmin, tmax) is blocked.
+__device__ __forceinline__ bool trav_begin(TravState& s, const TraceScene& sc, V3 o, V3 d, float tmin, float tmax,
+                                           bool any = false) {
+  s.any = any;
   s.best_t = tmax;
   s.cull = tmax;
   s.best_prim = -1;
@@ -479,10 +485,28 @@ __device__ __forceinline__ void trav_tris_warp(TravState& s, const TraceScene& s
   __syncwarp();
 }
 
+// Whether the ray may meet the box [lo, hi] inside (tmin, tmax): slab
+// distances from the node-culling reciprocals, each widened by 2^-20 of
+// their magnitude, which covers their roundings (conservative: a ray that
+// meets the box is never rejected).
+__device__ __forceinline__ bool box_may_hit(const RayPre& r, const float* lo, const float* hi, float tmin,
+                                            float tmax) {
+  const float ax = (lo[0] - r.ox) * r.ix, bx = (hi[0] - r.ox) * r.ix;
+  const float ay = (lo[1] - r.oy) * r.iy, by = (hi[1] - r.oy) * r.iy;
+  const float az = (lo[2] - r.oz) * r.iz, bz = (hi[2] - r.oz) * r.iz;
+  const float gx = 9.5367431640625e-7f * (fabsf(ax) + fabsf(bx));
+  const float gy = 9.5367431640625e-7f * (fabsf(ay) + fabsf(by));
+  const float gz = 9.5367431640625e-7f * (fabsf(az) + fabsf(bz));
+  const float tn = fmaxf(fmaxf(fminf(ax, bx) - gx, fminf(ay, by) - gy), fmaxf(fminf(az, bz) - gz, tmin));
+  const float tf = fminf(fminf(fmaxf(ax, bx) + gx, fmaxf(ay, by) + gy), fminf(fmaxf(az, bz) + gz, tmax));
+  return tn <= tf;
+}
+
 // Orders the children trav_node pushed by entry distance (nearest on top)
 // and moves to the nearest child not culled.  Returns true when the
 // traversal is finished.
 __device__ __forceinline__ bool trav_pop(TravState& s, uint2* stack, int sp0) {
+  if (s.any && s.best_prim >= 0) return true;
   // (entry distances are positive, so their bit patterns order as floats)
   const int sp = s.sp;
   for (int i = sp0 + 1; i < sp; ++i) {

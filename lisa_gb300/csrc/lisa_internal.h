@@ -146,6 +146,8 @@ struct SceneGpu {
   float4* emit = nullptr;       // physically based estimator: emitter records
   float* emit_cdf = nullptr;
   uint32_t num_emit = 0;
+  bool has_emit_box = false;  // bounds of the emissive triangles (padded), for the emitter search
+  float emit_lo[3] = {0, 0, 0}, emit_hi[3] = {0, 0, 0};
   float extent = 0.0f;
   float eye[3], U[3], V[3], W[3];
   int guide = -1;

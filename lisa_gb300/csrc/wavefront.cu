@@ -487,6 +487,10 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
         dir = bsdf::shoot_ray_hemisphere(N, seed);
         ++shadow;
         ray_active = trav_begin(s, ts, v3(s.r.ox, s.r.oy, s.r.oz), dir, RAY_TMIN, RAY_TMAX);
+        // a ray that cannot reach an emitter only needs to know whether it
+        // hits anything (a miss clears the flag, another hit keeps it), so
+        // its traversal ends at the first hit
+        if (ray_active) s.any = !(sc->has_emit_box && box_may_hit(s.r, sc->emit_lo, sc->emit_hi, RAY_TMIN, RAY_TMAX));
         pending = !ray_active;  // nothing to traverse: a miss
       }
     }
@@ -689,8 +693,8 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
                 em_m = __float_as_int(__ldg(sc->emit + 4ull * k + 1).w);
                 shadow = true;
                 ++nshadow;
-                // stop short of the emitter itself
-                ray_active = trav_begin(s, ts, p, wi, RAY_TMIN, fmul(dist, 0.9990234375f));
+                // stop short of the emitter itself; any blocker will do
+                ray_active = trav_begin(s, ts, p, wi, RAY_TMIN, fmul(dist, 0.9990234375f), true);
               }
             }
             pending = !ray_active;  // no shadow ray, or nothing to traverse
