@@ -38,7 +38,7 @@ namespace lisa {
 constexpr uint32_t FULL = 0xffffffffu;
 
 #ifndef LISA_NEE_MIN_BLOCKS
-#define LISA_NEE_MIN_BLOCKS 8  // 8 x 128 threads per SM (64 registers; measured best of 6..10)
+#define LISA_NEE_MIN_BLOCKS 7  // 7 x 128 threads per SM (72 registers; measured best of 6..10)
 #endif
 #ifndef LISA_NEE_PB_MIN_BLOCKS
 #define LISA_NEE_PB_MIN_BLOCKS 7  // physically based emitter kernel: 7 x 128 threads per SM
