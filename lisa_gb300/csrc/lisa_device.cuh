@@ -150,15 +150,6 @@ __device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
   r.ox = o.x;
   r.oy = o.y;
   r.oz = o.z;
-  // __frcp_rn is the correctly rounded 1/x, the same value as 1.0f/x.  A
-  // zero component takes a huge finite reciprocal of its sign instead of
-  // infinity: the node test then keeps that axis's slab (the ray's constant
-  // coordinate against the padded box) instead of turning it into NaN and
-  // dropping it, which made such rays visit most of the tree.  Only node
-  // culling reads these; the triangle test uses the shear constants.
-  r.ix = d.x != 0.0f ? __frcp_rn(d.x) : copysignf(1e30f, d.x);
-  r.iy = d.y != 0.0f ? __frcp_rn(d.y) : copysignf(1e30f, d.y);
-  r.iz = d.z != 0.0f ? __frcp_rn(d.z) : copysignf(1e30f, d.z);
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
   int kx = kz + 1;
@@ -174,7 +165,21 @@ __device__ __forceinline__ RayPre ray_prepare(V3 o, V3 d, float extent) {
   r.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
   r.Sx = fdiv(sel3(d.x, d.y, d.z, kx), dz);
   r.Sy = fdiv(sel3(d.x, d.y, d.z, ky), dz);
+  // __frcp_rn is the correctly rounded 1/x, the same value as 1.0f/x: the
+  // shear's 1/dz, and the node-culling reciprocal of that (dominant) axis
   r.Sz = __frcp_rn(dz);
+  // The other two axes' reciprocals serve node culling only; __fdividef is
+  // within 2 ulp there, which the slab padding covers (see trav_node).  A
+  // zero or vanishing component takes a huge finite reciprocal of its sign
+  // instead of infinity: the node test then keeps that axis's slab (the
+  // ray's constant coordinate against the padded box) instead of turning it
+  // into NaN and dropping it, which made such rays visit most of the tree.
+  const float qx = ax > 1e-30f ? __fdividef(1.0f, d.x) : copysignf(1e30f, d.x);
+  const float qy = ay > 1e-30f ? __fdividef(1.0f, d.y) : copysignf(1e30f, d.y);
+  const float qz = az > 1e-30f ? __fdividef(1.0f, d.z) : copysignf(1e30f, d.z);
+  r.ix = kz == 0 ? r.Sz : qx;
+  r.iy = kz == 1 ? r.Sz : qy;
+  r.iz = kz == 2 ? r.Sz : qz;
   // 2^-18 * extent / |d|max; a margin, so an approximate quotient will do
   r.slack = __fdividef(3.814697265625e-6f * extent, fmaxf(ax, fmaxf(ay, az)));
   return r;
@@ -212,9 +217,11 @@ __device__ __forceinline__ float intersect_tri(const RayPre& r, float4 a4, float
 // Closest-hit traversal of the 8-wide compressed BVH, one node per step.
 //
 // Box tests are made conservative by padding each slab distance by
-// 2^-21 (|c| + 255 |s|), which bounds the rounding of q*s + c with
-// s = 2^e/d and c = (p-o)/d, so the traversal never culls a box the exact
-// ray enters.  Candidates are culled against best_t*(1+2^-16) + slack.
+// 2^-20 (|c| + 255 |s|), which bounds the rounding of q*s + c with
+// s = 2^e/d and c = (p-o)/d -- 1/d within 2 ulp, p-o, the product, the fma
+// and the padding's own subtraction: about 9 * 2^-24 (|c| + 255 |s|) in all,
+// against 16 * 2^-24 -- so the traversal never culls a box the exact ray
+// enters.  Candidates are culled against best_t*(1+2^-16) + slack.
 // Together with the lowest-index tie rule the result equals a brute-force
 // scan with the same triangle test.
 //
@@ -304,9 +311,9 @@ __device__ __forceinline__ NodeWork trav_node(TravState& s, const TraceScene& sc
   const float cx = (__uint_as_float(n0.x) - r.ox) * r.ix;
   const float cy = (__uint_as_float(n0.y) - r.oy) * r.iy;
   const float cz = (__uint_as_float(n0.z) - r.oz) * r.iz;
-  const float gx = 4.76837158203125e-7f * (fabsf(cx) + 255.0f * fabsf(sx));
-  const float gy = 4.76837158203125e-7f * (fabsf(cy) + 255.0f * fabsf(sy));
-  const float gz = 4.76837158203125e-7f * (fabsf(cz) + 255.0f * fabsf(sz));
+  const float gx = 9.5367431640625e-7f * (fabsf(cx) + 255.0f * fabsf(sx));
+  const float gy = 9.5367431640625e-7f * (fabsf(cy) + 255.0f * fabsf(sy));
+  const float gz = 9.5367431640625e-7f * (fabsf(cz) + 255.0f * fabsf(sz));
   const float cnx = cx - gx, cfx = cx + gx;
   const float cny = cy - gy, cfy = cy + gy;
   const float cnz = cz - gz, cfz = cz + gz;
