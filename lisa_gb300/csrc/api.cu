@@ -582,15 +582,15 @@ void lisa_options_default(lisa_options* o) {
   o->use_graph = 1;
   o->guide_bsdf_fraction = 0.5f;
   // 128 Adam steps of one 128-sample tile per SM (19,456 samples on 152
-  // SMs) per 4 Mi paths at lr 1e-3, up to 1024 steps per scene, after 4
+  // SMs) per 4 Mi paths at lr 1e-3, up to 2048 steps per scene, after 2
   // warm-up waves, with at most 16 spp per wave
   o->guide_lr = 1e-3f;
   o->guide_train_batch = 0;
-  o->guide_warmup_waves = 4;
+  o->guide_warmup_waves = 2;
   o->guide_steps_per_wave = 128;
   o->guide_spp_per_wave = 16;
   o->guide_min_spp = 256;  // below that, warm-up waves would take most of the render
-  o->guide_train_steps = 1024;
+  o->guide_train_steps = 2048;
 }
 
 int lisa_renderer_create(const lisa_renderer_params* params, const lisa_options* opts, lisa_renderer** out) {

@@ -63,11 +63,15 @@ __device__ __forceinline__ void pack_store(uint16_t* pack, int row, int col, flo
 // are written in place (the zero padding rows never change), and the summed
 // loss goes to loss_last.  The step count lives on the device (the training kernel
 // increments it), so a captured graph replays with the right bias
-// correction.
+// correction.  With `count`, the step is skipped when the training slice
+// that starts at `first` had no sample (a wave that gathered fewer samples
+// than its steps would use): momentum alone would keep moving the weights.
 __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
                              const float* __restrict__ part, const float* __restrict__ loss_part, uint32_t nparts,
                              float* __restrict__ loss_last, float lr, const uint32_t* __restrict__ step,
-                             uint32_t* status, uint16_t* __restrict__ pack) {
+                             uint32_t* status, uint16_t* __restrict__ pack, const uint32_t* __restrict__ count,
+                             uint32_t first) {
+  if (count && *(volatile const uint32_t*)count <= first) return;
   // four threads per parameter (neighbouring lanes) each sum every fourth
   // partial slot; the sums meet by shuffles
   const int t4 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -208,7 +212,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   // samples [src.first, n)
   const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
   const uint32_t ntiles = (n - src.first + 127) / 128;
-  if (step_bump && blockIdx.x == 0 && threadIdx.x == 0) *step_bump += 1;  // the Adam step that follows
+  // the Adam step that follows (none for an empty slice)
+  if (step_bump && n > src.first && blockIdx.x == 0 && threadIdx.x == 0) *step_bump += 1;
   float* slot = part + (size_t)blockIdx.x * NPARAM;  // this CTA's partial gradient
   if (blockIdx.x >= ntiles) {
     for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) slot[k] = 0.0f;
@@ -543,9 +548,9 @@ Status guide_launch_reduce(GuideNet& g, cudaStream_t s) {
   return Status();
 }
 
-Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
+Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s, const uint32_t* count, uint32_t first) {
   k_guide_adam<<<(4 * NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grad_part, g.loss_part, g.nparts,
-                                                    g.loss_last, lr, g.d_step, g.status, g.w_bf16);
+                                                    g.loss_last, lr, g.d_step, g.status, g.w_bf16, count, first);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }

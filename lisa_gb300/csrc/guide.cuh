@@ -74,7 +74,8 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float 
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s);
 // Adam step on the summed partials; also refreshes the BF16 weights and
 // moves the loss to loss_last
-Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s);
+// With `count`: skipped on the device when the slice starting at `first` is empty.
+Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s, const uint32_t* count = nullptr, uint32_t first = 0);
 Status guide_check_status(GuideNet& g, cudaStream_t s);
 Status guide_renderer_init(Renderer& r);
 // Shared-memory attributes of the renderer's fused inference kernels (wavefront.cu).

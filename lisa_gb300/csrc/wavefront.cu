@@ -1293,7 +1293,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
           return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream,
                                     true);
         }));
-        LISA_TRY(stage(4, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream); }));
+        LISA_TRY(stage(4, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream, slice.count, slice.first); }));
       }
     }
   }

@@ -54,8 +54,8 @@ def test_hard_indirect_guided_vs_plain(gpu, capsys):
     """Hard-indirect scene (0.02 x 0.02 light behind a baffle), 128 x 128,
     1024 spp: relMSE of plain and guided renders at the same spp against a
     32k-spp plain reference.  The guide trains online (4 warm-up waves that
-    sample the BSDF only, 16 Adam steps after each wave of 16 spp).  Training
-    order is not deterministic (gradient atomics), so the check is a
+    sample the BSDF only, 16 Adam steps after each wave of 16 spp).  The
+    order of training samples is not deterministic (atomics), so the check is a
     regression bound -- guided within 15 % of plain -- and both numbers are
     printed."""
     sc = scenes.hard_indirect(level=5, width=128, height=128, num_samples=1024, num_bounces=8)
