@@ -42,6 +42,24 @@ def test_path_by_path_cornell_box(gpu, oracle):
     assert st.device_status == 0
 
 
+def test_path_by_path_hard_indirect(gpu, oracle):
+    """A 0.02 x 0.02 light behind a baffle: almost every emitter-search ray
+    misses the padded bounds of the emissive triangles and stops at its
+    first hit, the rest keep the closest-hit traversal; the search's
+    outcomes (and so the paths) must equal the oracle's closest-hit scan."""
+    sc = scenes.hard_indirect(level=4, width=32, height=32, num_samples=4, num_bounces=8)
+    r = L.Renderer(L.params_from_scene(sc))
+    st = r.render()
+    img = r.image()
+    ref, _, rays = oracle_mean(oracle, sc)
+    assert mismatch_fraction(img, ref) <= 0.002
+    assert st.rays_primary == rays[0]
+    assert abs(int(st.rays_bounce) - int(rays[1])) <= 0.002 * rays[1]
+    assert abs(int(st.rays_shadow) - int(rays[2])) <= 0.002 * rays[2]
+    assert st.device_status == 0
+    assert img.max() > 0
+
+
 def test_path_by_path_reference_stream(gpu, oracle):
     """LISA_RNG_PER_PIXEL: one tea<16>(pixel, subframe) stream per pixel
     shared by its samples, exactly the reference raygen (shader.cu:141-155)."""
