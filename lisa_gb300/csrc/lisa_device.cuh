@@ -509,6 +509,28 @@ __device__ __forceinline__ bool box_may_hit(const RayPre& r, const float* lo, co
   return tn <= tf;
 }
 
+// Whether the ray (o, d) may meet the box [lo, hi] inside (tmin, tmax),
+// every step a single IEEE rounding so the host oracle takes the same
+// decision bit for bit: slab distances with the correctly rounded 1/d (a
+// huge finite value of d's sign for a zero component), each widened by
+// 2^-20 of their magnitude.  Used where a ray is traced only for the
+// emission it may reach: one that misses the emissive triangles' padded
+// bounds would gather nothing, so it is not traced at all.
+__device__ __forceinline__ bool box_may_hit_exact(V3 o, V3 d, const float* lo, const float* hi, float tmin,
+                                                  float tmax) {
+  const float dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
+  float tn = tmin, tf = tmax;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float inv = dd[k] != 0.0f ? __frcp_rn(dd[k]) : copysignf(1e30f, dd[k]);
+    const float a = fmul(fsub(lo[k], oo[k]), inv), b = fmul(fsub(hi[k], oo[k]), inv);
+    const float g = fmul(9.5367431640625e-7f, fadd(fabsf(a), fabsf(b)));
+    tn = fmaxf(tn, fsub(fminf(a, b), g));
+    tf = fminf(tf, fadd(fmaxf(a, b), g));
+  }
+  return tn <= tf;
+}
+
 // Orders the children trav_node pushed by entry distance (nearest on top)
 // and moves to the nearest child not culled.  Returns true when the
 // traversal is finished.

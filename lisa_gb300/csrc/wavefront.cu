@@ -71,6 +71,12 @@ __device__ __forceinline__ void warp_add64(unsigned long long* c, uint32_t v) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(c, (unsigned long long)v);
 }
 
+// The ray leaving a path's last vertex (physically based estimator) only
+// gathers emission: it is traced only if it may meet the scene's emitters.
+__device__ __forceinline__ bool final_ray_wanted(const SceneDev& sc, V3 p, V3 d) {
+  return sc.has_emit_box && box_may_hit_exact(p, d, sc.emit_lo, sc.emit_hi, RAY_TMIN, RAY_TMAX);
+}
+
 __device__ __forceinline__ void warp_add32(uint32_t* c, uint32_t v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(c, v);
@@ -331,6 +337,7 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
             b.ps_rng[slot] = seed;
             b.ps_att[slot] = make_float4(a.x, a.y, a.z, PHYS ? 0.0f : att.w);
             want_ray = !last && !is_zero(nd);
+            if (PHYS && want_ray && depth + 1 == (int)sc.num_bounces) want_ray = final_ray_wanted(sc, p, nd);
           } else {
             const V3 a = ld3(att) * v3(m.albedo[0], m.albedo[1], m.albedo[2]);
             b.ps_att[slot] = make_float4(a.x, a.y, a.z, att.w);
@@ -642,6 +649,8 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
             nd = reflect(ld3(b.nee_c[entry]), Ns);
           }
           want_ray = !is_zero(nd);
+          if (want_ray && depth + 1 == (int)sc->num_bounces)
+            want_ray = final_ray_wanted(*sc, v3(s.r.ox, s.r.oy, s.r.oz), nd);
           b.ps_rng[slot] = seed;
           b.ps_att[slot] = make_float4(att.x, att.y, att.z, prev);
         }
@@ -776,6 +785,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
     nd = reflect(D, Ns);
     want = true;
   }
+  if (want && depth + 1 == (int)sc.num_bounces) want = final_ray_wanted(sc, p, nd);
   b.ps_col[slot] = make_float4(col.x, col.y, col.z, cw.w);
   b.ps_rng[slot] = seed;
   b.ps_att[slot] = make_float4(att.x, att.y, att.z, prev);

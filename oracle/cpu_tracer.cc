@@ -234,6 +234,10 @@ struct Ctx {
   Bvh bvh;
   bool use_bvh = false;
   Emitters em;
+  // bounds of the emissive triangles, padded by 1e-4 of the scene diagonal
+  // (the same float steps as the product's scene upload)
+  bool has_emit_box = false;
+  float emit_lo[3] = {0, 0, 0}, emit_hi[3] = {0, 0, 0};
 };
 
 void build_bvh(Ctx& c) {
@@ -548,6 +552,26 @@ uint32_t sample_emitter(const Emitters& e, uint32_t& seed, V3& y) {
   return lo;
 }
 
+// Whether the ray may meet the padded bounds of the emissive triangles in
+// (1e-4, 1e16): slab distances with the correctly rounded 1/d (a huge
+// finite value for a zero component), widened by 2^-20 of their magnitude.
+// The ray leaving a path's last vertex only gathers emission, so one that
+// cannot meet an emitter is not traced (the product takes the same
+// decision with the same float steps).
+bool final_ray_wanted(const Ctx& c, V3 o, V3 d) {
+  if (!c.has_emit_box) return false;
+  const float dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
+  float tn = 1e-4f, tf = 1e16f;
+  for (int k = 0; k < 3; ++k) {
+    const float inv = dd[k] != 0.0f ? 1.0f / dd[k] : std::copysign(1e30f, dd[k]);
+    const float a = (c.emit_lo[k] - oo[k]) * inv, b = (c.emit_hi[k] - oo[k]) * inv;
+    const float g = 9.5367431640625e-7f * (std::fabs(a) + std::fabs(b));
+    tn = std::fmax(tn, std::fmin(a, b) - g);
+    tf = std::fmin(tf, std::fmax(a, b) + g);
+  }
+  return tn <= tf;
+}
+
 // One path of the physically based estimator.
 V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters& cnt) {
   V3 color = v3(0.0f, 0.0f, 0.0f), att = v3(1.0f, 1.0f, 1.0f);
@@ -558,6 +582,7 @@ V3 trace_path_pb(const Ctx& c, V3 o, V3 d, int bounces, uint32_t& seed, Counters
   // emitter sample), with no vertex of its own
   for (int i = 0; i <= bounces; ++i) {
     if (is_zero(d)) break;
+    if (i == bounces && i > 0 && !final_ray_wanted(c, o, d)) break;
     if (i == 0) ++cnt.primary; else ++cnt.bounce;
     int prim;
     float t;
@@ -722,6 +747,27 @@ static void make_ctx(const oracle_scene* s, int use_bvh, Ctx& c) {
   c.use_bvh = use_bvh != 0;
   if (c.use_bvh) build_bvh(c);
   if (c.mi) build_emitters(c);
+  if (c.mi && c.T) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    float ext = std::sqrt(dx * dx + dy * dy + dz * dz);
+    if (!(ext > 0.0f) || !std::isfinite(ext)) ext = 1.0f;
+    float elo[3] = {INF, INF, INF}, ehi[3] = {-INF, -INF, -INF};
+    for (uint32_t t = 0; t < c.T; ++t) {
+      const int32_t m = c.mi[t];
+      if (m < 0 || m >= (int32_t)c.cls.size() || c.cls[m] != 2) continue;
+      c.has_emit_box = true;
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          elo[k] = std::min(elo[k], c.v[9ull * t + 3 * j + k]);
+          ehi[k] = std::max(ehi[k], c.v[9ull * t + 3 * j + k]);
+        }
+    }
+    const float pad = 1e-4f * ext;
+    for (int k = 0; k < 3; ++k) {
+      c.emit_lo[k] = c.has_emit_box ? elo[k] - pad : 0.0f;
+      c.emit_hi[k] = c.has_emit_box ? ehi[k] + pad : 0.0f;
+    }
+  }
 }
 
 // Closest hit of n rays (8 floats each: ox oy oz tmin dx dy dz tmax).
