@@ -409,6 +409,10 @@ Status renderer_create(const lisa_renderer_params* scenes, int n, const lisa_opt
   if (r->opts.mode > LISA_MODE_GUIDED) return Status::invalid("unknown mode");
   if (r->opts.rng > LISA_RNG_PER_PIXEL) return Status::invalid("unknown rng mode");
   if (r->opts.estimator > LISA_ESTIMATOR_PHYSICAL) return Status::invalid("unknown estimator");
+  // the persistent traversal kernels work on whole warps, at most 4 per block
+  if (r->opts.threads_per_block % 32u || r->opts.threads_per_block > 128u)
+    return Status::invalid("threads_per_block: 0 (auto) or a multiple of 32 up to 128");
+  if (r->opts.refill_idle > 32u) return Status::invalid("refill_idle: 0 (default) or 1..32");
   r->arena.cap = r->opts.alloc_cap_bytes;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);

@@ -52,6 +52,27 @@ def test_errors_without_gpu_are_reported_not_raised():
     assert lib.lisa_render(None, None) == N.LISA_ERR_INVALID
 
 
+def test_renderer_options_are_checked_before_the_device():
+    """Launch and mode options out of range are refused as invalid before
+    any device is touched (a block size that is not whole warps, or above
+    the persistent kernels' 128 threads, would break their warp-wide
+    steps)."""
+    import numpy as np
+    import pytest
+
+    import lisa_gb300 as L
+
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    n = np.tile(np.array([0, 0, 1], np.float32), (3, 1))
+    mats = np.array([[1, 1, 1, 0.5, 0.5, 0.5, 0, 0, 0, 0]], np.float32)
+    p = L.params_from_arrays(v, n, np.zeros(1, np.int32), mats, 4, 4, (0, 0, 2), (0, 0, 0), 40.0, 1, 2)
+    for kw in (dict(threads_per_block=100), dict(threads_per_block=256), dict(refill_idle=33),
+               dict(estimator=9), dict(mode=7)):
+        with pytest.raises(N.LisaError) as e:
+            L.Renderer(p, **kw)
+        assert e.value.code == N.LISA_ERR_INVALID, kw
+
+
 def test_ppm_writer_matches_save_image_layout(tmp_path):
     import numpy as np
 
