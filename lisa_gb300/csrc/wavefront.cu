@@ -970,17 +970,26 @@ __global__ void k_tonemap(const float4* __restrict__ sum, uint32_t npix, float i
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_rays(const SceneDev* __restrict__ scd, const float* __restrict__ rays,
                                                    uint32_t n, int32_t* prim, float* tout, WaveCtrl* ctrl) {
+  // the same warp-wide traversal step as the wavefront kernels (whole
+  // warps run each round: `total` is a multiple of 32, as is the stride)
   uint32_t visits = 0, tests = 0;
+  __shared__ TriPass tri_pass[4];
+  TriPass& tp = tri_pass[threadIdx.x >> 5];
+  uint2 stack[TRAV_STACK];
+  const TraceScene ts = trace_scene(*scd);
   const uint32_t total = ((n + 31) / 32) * 32;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    TravState s;
+    bool active = false;
     if (i < n) {
       const float* r = rays + 8ull * i;
-      int hp;
-      float ht;
-      closest_hit<COUNT>(trace_scene(*scd), v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7], hp, ht, visits,
-                         tests, &ctrl->status);
-      if (prim) prim[i] = hp;
-      if (tout) tout[i] = ht;
+      active = trav_begin(s, ts, v3(r[0], r[1], r[2]), v3(r[4], r[5], r[6]), r[3], r[7]);
+    }
+    while (__any_sync(FULL, active))
+      if (trav_step_warp<COUNT>(active, s, ts, stack, visits, tests, &ctrl->status, tp)) active = false;
+    if (i < n) {
+      if (prim) prim[i] = s.best_prim;
+      if (tout) tout[i] = s.best_prim >= 0 ? s.best_t : __int_as_float(0x7f800000);
     }
   }
   if (COUNT) {
