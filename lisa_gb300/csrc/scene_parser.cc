@@ -26,10 +26,15 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 namespace lisa {
 
@@ -418,12 +423,64 @@ inline int split_tokens(const char* p, const char* e, const char** tb, const cha
 
 }  // namespace
 
-Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx) {
-  std::string data;
-  if (!read_whole_file(path, &data)) return Status::io(path + " not found.");
-  const char* base = data.data();
-  const size_t n = data.size();
-  unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+namespace {
+
+// One OBJ file as a de-indexed soup: three vertices and three normals per
+// face.  A file of at least 1 MB is split over up to `max_threads` threads.
+struct ObjSoup {
+  std::vector<lisa_float3> vertices, normals;
+};
+
+// Runs fn(t) for t in [0, n): on this thread when n is 1.
+template <class F>
+void run_threads(unsigned n, F&& fn) {
+  if (n <= 1) {
+    fn(0u);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < n; ++t) th.emplace_back([&fn, t] { fn(t); });
+  for (auto& x : th) x.join();
+}
+
+// The whole file into an uninitialised buffer; a file of at least 8 MB is
+// read by `nth` threads, each its own byte range (pread).
+bool read_file_parallel(const std::string& path, unsigned nth, std::unique_ptr<char[]>* buf, size_t* size) {
+  const int fd = ::open(path.c_str(), O_RDONLY);
+  if (fd < 0) return false;
+  struct stat sb;
+  if (::fstat(fd, &sb) != 0 || sb.st_size < 0) {
+    ::close(fd);
+    return false;
+  }
+  const size_t n = (size_t)sb.st_size;
+  buf->reset(new char[n > 0 ? n : 1]);
+  if (n < (8u << 20)) nth = 1;
+  std::atomic<bool> ok{true};
+  run_threads(nth, [&](unsigned t) {
+    size_t off = n * t / nth;
+    const size_t end = n * (t + 1) / nth;
+    while (off < end) {
+      const ssize_t r = ::pread(fd, buf->get() + off, end - off, (off_t)off);
+      if (r <= 0) {
+        ok = false;
+        return;
+      }
+      off += (size_t)r;
+    }
+  });
+  ::close(fd);
+  *size = n;
+  return ok;
+}
+
+Status obj_parse(const std::string& path, unsigned max_threads, ObjSoup& out) {
+  std::unique_ptr<char[]> data;
+  size_t n = 0;
+  if (!read_file_parallel(path, std::max(1u, std::min(64u, max_threads)), &data, &n))
+    return Status::io(path + " not found.");
+  const char* base = data.get();
+  unsigned nth = std::max(1u, std::min(64u, max_threads));
   if (n < (1u << 20)) nth = 1;
   std::vector<ObjChunk> ch(nth);
   for (unsigned t = 0; t < nth; ++t) {
@@ -450,20 +507,15 @@ Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx) {
     return true;
   };
   // pass 1: count records per chunk
-  {
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nth; ++t)
-      th.emplace_back([&, t] {
-        for_lines(ch[t], [&](const char* p, const char* e) {
-          int k = line_kind(p, e);
-          if (k == LINE_V) ch[t].nv++;
-          else if (k == LINE_VN) ch[t].nn++;
-          else if (k == LINE_F) ch[t].nf++;
-          return true;
-        });
-      });
-    for (auto& x : th) x.join();
-  }
+  run_threads(nth, [&](unsigned t) {
+    for_lines(ch[t], [&](const char* p, const char* e) {
+      int k = line_kind(p, e);
+      if (k == LINE_V) ch[t].nv++;
+      else if (k == LINE_VN) ch[t].nn++;
+      else if (k == LINE_F) ch[t].nf++;
+      return true;
+    });
+  });
   std::vector<size_t> ov(nth + 1, 0), on(nth + 1, 0), of(nth + 1, 0);
   for (unsigned t = 0; t < nth; ++t) {
     ov[t + 1] = ov[t] + ch[t].nv;
@@ -476,9 +528,7 @@ Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx) {
   std::vector<std::string> errs(nth);
   // pass 2: parse in place
   {
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nth; ++t)
-      th.emplace_back([&, t] {
+    run_threads(nth, [&](unsigned t) {
         size_t iv = ov[t], in = on[t], iff = of[t];
         bool ok = for_lines(ch[t], [&](const char* p, const char* e) {
           int k = line_kind(p, e);
@@ -527,7 +577,6 @@ Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx) {
         });
         if (!ok) bad = true;
       });
-    for (auto& x : th) x.join();
   }
   if (bad) {
     for (auto& e : errs)
@@ -535,32 +584,91 @@ Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx) {
   }
   // de-index (parse_obj.cc:56-61)
   const size_t nfaces = of[nth];
-  const size_t v0 = sc.vertices.size();
-  sc.vertices.resize(v0 + 3 * nfaces);
-  sc.normals.resize(v0 + 3 * nfaces);
-  sc.mat_indices.resize(sc.mat_indices.size() + nfaces, mat_idx);
+  out.vertices.resize(3 * nfaces);
+  out.normals.resize(3 * nfaces);
   const long nvt = (long)ov[nth], nnt = (long)on[nth];
   std::atomic<bool> range_bad{false};
-  {
-    std::vector<std::thread> th;
-    unsigned nt2 = nfaces > 100000 ? nth : 1;
-    for (unsigned t = 0; t < nt2; ++t)
-      th.emplace_back([&, t] {
-        size_t b = nfaces * t / nt2, e = nfaces * (t + 1) / nt2;
-        for (size_t f = b; f < e; ++f)
-          for (int c = 0; c < 3; ++c) {
-            long a = fv[3 * f + c], q = fn[3 * f + c];
-            if (a < 0 || a >= nvt || q < 0 || q >= nnt) {
-              range_bad = true;
-              return;
-            }
-            sc.vertices[v0 + 3 * f + c] = {vt[3 * a], vt[3 * a + 1], vt[3 * a + 2]};
-            sc.normals[v0 + 3 * f + c] = {nt[3 * q], nt[3 * q + 1], nt[3 * q + 2]};
-          }
-      });
-    for (auto& x : th) x.join();
-  }
+  const unsigned nt2 = nfaces > 100000 ? nth : 1;
+  run_threads(nt2, [&](unsigned t) {
+    size_t b = nfaces * t / nt2, e = nfaces * (t + 1) / nt2;
+    for (size_t f = b; f < e; ++f)
+      for (int c = 0; c < 3; ++c) {
+        long a = fv[3 * f + c], q = fn[3 * f + c];
+        if (a < 0 || a >= nvt || q < 0 || q >= nnt) {
+          range_bad = true;
+          return;
+        }
+        out.vertices[3 * f + c] = {vt[3 * a], vt[3 * a + 1], vt[3 * a + 2]};
+        out.normals[3 * f + c] = {nt[3 * q], nt[3 * q + 1], nt[3 * q + 2]};
+      }
+  });
   if (range_bad) return Status::parse(path + ": face index out of range");
+  return Status();
+}
+
+unsigned host_threads() { return std::max(1u, std::min(64u, std::thread::hardware_concurrency())); }
+
+void soup_append(Scene& sc, const ObjSoup& o, int32_t mat_idx) {
+  sc.vertices.insert(sc.vertices.end(), o.vertices.begin(), o.vertices.end());
+  sc.normals.insert(sc.normals.end(), o.normals.begin(), o.normals.end());
+  sc.mat_indices.resize(sc.mat_indices.size() + o.vertices.size() / 3, mat_idx);
+}
+
+// The OBJ files of a scene's meshes, appended in declaration order.  Files
+// under 1 MB are parsed side by side, one file per thread (a scene of many
+// small meshes); larger ones one at a time on all threads.  The error
+// reported is that of the first failing file in declaration order, as the
+// reference, which loads them one after the other, would report.
+struct ObjJob {
+  std::string path;
+  int32_t mat_idx;
+};
+
+Status obj_append_all(Scene& sc, const std::vector<ObjJob>& jobs) {
+  const size_t n = jobs.size();
+  std::vector<ObjSoup> soups(n);
+  std::vector<Status> st(n);
+  std::vector<size_t> small, large;
+  for (size_t i = 0; i < n; ++i) {
+    FILE* f = std::fopen(jobs[i].path.c_str(), "rb");
+    long sz = 0;
+    if (f) {
+      std::fseek(f, 0, SEEK_END);
+      sz = std::ftell(f);
+      std::fclose(f);
+    }
+    (sz >= (1l << 20) ? large : small).push_back(i);
+  }
+  const unsigned nth = host_threads();
+  std::atomic<size_t> next{0};
+  run_threads(std::min<size_t>(nth, small.size()), [&](unsigned) {
+    for (size_t k = next++; k < small.size(); k = next++) {
+      const size_t i = small[k];
+      st[i] = obj_parse(jobs[i].path, 1, soups[i]);
+    }
+  });
+  for (size_t i : large) st[i] = obj_parse(jobs[i].path, nth, soups[i]);
+  for (size_t i = 0; i < n; ++i)
+    if (!st[i].ok()) return st[i];
+  size_t tv = sc.vertices.size();
+  for (const ObjSoup& o : soups) tv += o.vertices.size();
+  sc.vertices.reserve(tv);
+  sc.normals.reserve(tv);
+  sc.mat_indices.reserve(tv / 3);
+  for (size_t i = 0; i < n; ++i) {
+    soup_append(sc, soups[i], jobs[i].mat_idx);
+    ObjSoup().vertices.swap(soups[i].vertices);  // free as we go
+    ObjSoup().normals.swap(soups[i].normals);
+  }
+  return Status();
+}
+
+}  // namespace
+
+Status obj_append(Scene& sc, const std::string& path, int32_t mat_idx) {
+  ObjSoup o;
+  LISA_TRY(obj_parse(path, host_threads(), o));
+  soup_append(sc, o, mat_idx);
   return Status();
 }
 
@@ -616,18 +724,28 @@ Status parse_scene_text(const std::string& raw, const std::string& base_dir, Sce
     }
   }
 
-  // meshes (scene_parser.cc:165-198)
+  // meshes (scene_parser.cc:165-198): declarations in order up to the first
+  // bad one, then their OBJ files; an OBJ error before that declaration
+  // comes first, as in the reference's one-by-one loading
+  std::vector<ObjJob> jobs;
+  Status decl;
   for (const Block& b : find_blocks(file, "mesh", false)) {
     const std::string s = file.substr(b.b, b.e - b.b);
     std::string mname;
-    if (!search_mesh_material(s, &mname))
-      return Status::parse("Error in mesh declaration: no valid material provided");
+    if (!search_mesh_material(s, &mname)) {
+      decl = Status::parse("Error in mesh declaration: no valid material provided");
+      break;
+    }
     auto it = sc.mat_name_idx.find(mname);
-    if (it == sc.mat_name_idx.end())
-      return Status::parse("Error in mesh declaration: " + mname + " material not found");
+    if (it == sc.mat_name_idx.end()) {
+      decl = Status::parse("Error in mesh declaration: " + mname + " material not found");
+      break;
+    }
     std::string path;
-    if (!search_obj_file(s, &path))
-      return Status::parse("Error in mesh declaration: no valid obj_file provided");
+    if (!search_obj_file(s, &path)) {
+      decl = Status::parse("Error in mesh declaration: no valid obj_file provided");
+      break;
+    }
     // The reference opens the path relative to the working directory.  A
     // relative path that does not exist there is also tried relative to the
     // directory of the .rto file.
@@ -636,8 +754,10 @@ Status parse_scene_text(const std::string& raw, const std::string& base_dir, Sce
       std::string alt = base_dir + "/" + path;
       if (file_exists(alt)) use = alt;
     }
-    if (!(st = obj_append(sc, use, it->second)).ok()) return st;
+    jobs.push_back({use, it->second});
   }
+  if (!(st = obj_append_all(sc, jobs)).ok()) return st;
+  if (!decl.ok()) return decl;
 
   // camera (scene_parser.cc:200-245)
   auto cams = find_blocks(file, "camera", false);

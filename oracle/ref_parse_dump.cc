@@ -9,8 +9,12 @@
 // field.  Floats are printed as their IEEE-754 bit patterns (hex) so the
 // comparison is bit exact.  Material fields the reference leaves
 // uninitialised (structs.hh:25-52) are not printed.
+// With --time as the first argument it parses the scene and prints only
+// the wall time of SceneParser + get_params in seconds (the reference's
+// front end, timed for oracle/parse_bench.py).
 #include "scene_parser.hh"
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -23,8 +27,16 @@ static uint32_t bits(float f) {
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    std::fprintf(stderr, "usage: %s scene.rto\n", argv[0]);
+    std::fprintf(stderr, "usage: %s [--time] scene.rto\n", argv[0]);
     return 2;
+  }
+  if (argc >= 3 && std::strcmp(argv[1], "--time") == 0) {
+    const auto t0 = std::chrono::steady_clock::now();
+    SceneParser timed(argv[2]);
+    RendererParams q = timed.get_params();
+    const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf("%.6f %d\n", s, q.num_vertices);
+    return 0;
   }
   SceneParser parser(argv[1]);
   RendererParams p = parser.get_params();

@@ -105,6 +105,16 @@ CASES = {
     "err_two_cameras": BASE.format(extra=PARAMS + "camera {\n position = (0,0,1)\n look_at = (0,0,0)\n fov = 40\n}\n"),
     "err_no_fov": BASE.replace("fov = 45", "fov = wide").format(extra=PARAMS),
     "err_missing_obj": BASE.replace("obj_file = tri.obj", "obj_file = nothing_here.obj").format(extra=PARAMS),
+    # the first failing mesh in declaration order decides the error (the
+    # product loads the OBJ files side by side)
+    "err_obj_before_material": BASE.replace("obj_file = quirks.obj", "obj_file = nothing_here.obj")
+                                   .replace("material = light", "material = wood").format(extra=PARAMS),
+    "err_material_before_obj": BASE.replace("material = glass", "material = wood")
+                                   .replace("obj_file = box.obj", "obj_file = nothing_here.obj").format(extra=PARAMS),
+    # many small meshes, materials cycling, appended in declaration order
+    "many_meshes": BASE.format(extra=PARAMS) + "".join(
+        f"mesh {{\n  obj_file = {('tri.obj', 'quirks.obj', 'box.obj')[k % 3]}\n"
+        f"  material = {('white', 'glass', 'light')[(k // 3) % 3]}\n}}\n" for k in range(60)),
 }
 
 
