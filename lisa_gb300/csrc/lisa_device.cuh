@@ -253,9 +253,11 @@ constexpr uint32_t NODE_NONE = 0xffffffffu;
 struct TravState {
   RayPre r;
   float tmin;
-  float best_t;
+  // (best_t and best_prim start defined: a lane without a ray still joins
+  // its warp's triangle pass, which reads them)
+  float best_t = 0.0f;
   float cull;  // best_t * (1+2^-16) + slack
-  int best_prim;
+  int best_prim = -1;
   int best_mat;  // emitter material of the best hit, -1 if not an emitter (from the leaf triangle)
   uint32_t node;
   int sp;
