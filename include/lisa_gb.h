@@ -362,6 +362,16 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
 /* The guide a renderer trains in guided mode (borrowed). */
 int lisa_renderer_guide(lisa_renderer* r, int32_t scene, lisa_guide** out);
 
+/* ---- diagnostics ---------------------------------------------------------- */
+
+/* Runs a kernel that waits, with `limit` polls, on an mbarrier that nothing
+ * completes -- the bounded-wait time-out path of the tensor-core kernels,
+ * taken on purpose -- and returns the device status word it left in
+ * *status_word (LISA_STATUS_WAIT_TIMEOUT set when the wait ran out).  The
+ * context stays usable afterwards. */
+#define LISA_STATUS_WAIT_TIMEOUT 16u
+int lisa_selftest_wait_timeout(uint32_t limit, uint32_t* status_word);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,7 @@ LISA_ERR_CUDA = 4
 LISA_ERR_OOM = 5
 LISA_ERR_DEVICE = 6
 LISA_ERR_UNSUPPORTED = 7
+LISA_STATUS_WAIT_TIMEOUT = 16  # device status bit: a bounded tensor-core wait ran out
 
 LISA_MODE_COMPAT = 0
 LISA_MODE_GUIDED = 1
@@ -141,6 +142,7 @@ SIGNATURES = {
     "lisa_tuning_cache_lookup": (C.c_int, [C.c_char_p, C.c_char_p, _P, C.POINTER(C.c_int32)]),
     "lisa_tuning_cache_store": (C.c_int, [C.c_char_p, _P]),
     "lisa_guide_create": (C.c_int, [C.c_uint32, C.POINTER(_P)]),
+    "lisa_selftest_wait_timeout": (C.c_int, [C.c_uint32, C.POINTER(C.c_uint32)]),
     "lisa_guide_destroy": (None, [_P]),
     "lisa_guide_get_params": (C.c_int, [_P, _P]),
     "lisa_guide_set_params": (C.c_int, [_P, _P]),

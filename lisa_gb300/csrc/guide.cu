@@ -612,7 +612,42 @@ static int gret(const Status& s) {
   return s.code;
 }
 
+// A barrier that nothing completes, waited on with an iteration limit: the
+// time-out path of the tensor-core kernels (status bit, early exit) taken
+// on purpose, with no fault and no unbounded wait.
+static_assert((ST_GUIDE_NONFINITE << 1) == LISA_STATUS_WAIT_TIMEOUT, "time-out status bit");
+
+__global__ void k_wait_timeout(uint32_t limit, uint32_t* status) {
+  __shared__ uint64_t mbar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&mbar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !tc::mbar_wait(&mbar, 0, limit)) atomicOr(status, ST_GUIDE_NONFINITE << 1);
+}
+
 extern "C" {
+
+int lisa_selftest_wait_timeout(uint32_t limit, uint32_t* status_word) {
+  if (!status_word || limit == 0) return gret(Status::invalid("null argument or zero limit"));
+  uint32_t* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return gret(Status(LISA_ERR_UNSUPPORTED, std::string("no CUDA device: ") + cudaGetErrorString(e)));
+  }
+  e = cudaMemset(d, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) {
+    k_wait_timeout<<<1, 32>>>(limit, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(status_word, d, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return gret(Status::cuda(e, "wait self-test"));
+  return gret(Status());
+}
 
 int lisa_guide_create(uint32_t seed, lisa_guide** out) {
   try {

@@ -50,6 +50,7 @@ def test_errors_without_gpu_are_reported_not_raised():
     assert lib.lisa_scene_parse(None, None) == N.LISA_ERR_INVALID
     assert b"null" in lib.lisa_last_error()
     assert lib.lisa_render(None, None) == N.LISA_ERR_INVALID
+    assert lib.lisa_selftest_wait_timeout(0, None) == N.LISA_ERR_INVALID
 
 
 def test_renderer_options_are_checked_before_the_device():
