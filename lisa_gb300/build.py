@@ -65,16 +65,46 @@ def _compile(src: str, extra=()):
 
 
 def build(verbose: bool = False, extra_flags=()) -> str:
+    """Compile and link the library.  extra_flags (e.g. ["-DLISA_BOUNDS"]
+    for the bounds-checked build) get their own object directory, so
+    switching between builds recompiles what they change; the library and
+    the CLI are relinked in place, so the last build wins."""
+    global BUILD
+    base = BUILD
+    if extra_flags:
+        import hashlib
+
+        BUILD = base + "_" + hashlib.sha1(" ".join(extra_flags).encode()).hexdigest()[:8]
+    try:
+        return _build(verbose, extra_flags)
+    finally:
+        BUILD = base
+
+
+def _build(verbose: bool, extra_flags) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(os.path.dirname(CLI), exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra_flags), srcs))
+    # which flags the library was last linked with: a switch relinks it
+    stamp = os.path.join(HERE, "_build", "last_link_flags")
+    flags = " ".join(extra_flags)
+    try:
+        with open(stamp) as f:
+            same = f.read() == flags
+    except OSError:
+        same = not flags
+    if not same and os.path.exists(LIB):
+        os.remove(LIB)
     if _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.makedirs(os.path.dirname(stamp), exist_ok=True)
+        with open(stamp, "w") as f:
+            f.write(flags)
     main = os.path.join(CSRC, "main.cc")
     if os.path.exists(main) and _stale(CLI, [main, LIB]):
         cmd = [nvcc()] + ARCH + COMMON + [main, "-o", CLI, "-L", HERE, "-llisa_gb",

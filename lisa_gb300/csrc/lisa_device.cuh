@@ -51,7 +51,15 @@ enum StatusBits : uint32_t {
   ST_QUEUE_OVERFLOW = 2u,
   ST_BAD_WAVE = 4u,
   ST_GUIDE_NONFINITE = 8u,
+  // 16: a bounded tensor-core wait ran out (LISA_STATUS_WAIT_TIMEOUT)
+  ST_BOUNDS = 32u,  // bounds-checked builds: a BVH or triangle index out of range
 };
+
+// Bounds-checked builds (-DLISA_BOUNDS, a stand-in for a memory checker):
+// node and triangle indices read from the BVH and the queue slots that
+// appends reserve are checked before use; a bad one sets a status bit and
+// the access is skipped.  Queue sizes are bounded by construction (one entry
+// per path and depth), so in ordinary builds the checks compile away.
 
 struct SceneDev {
   const uint4* nodes;
@@ -237,6 +245,9 @@ struct TraceScene {
   const float4* tris;
   uint32_t num_nodes;
   float extent;
+#ifdef LISA_BOUNDS
+  uint32_t num_tris;
+#endif
 };
 
 __device__ __forceinline__ TraceScene trace_scene(const SceneDev& sc) {
@@ -245,6 +256,9 @@ __device__ __forceinline__ TraceScene trace_scene(const SceneDev& sc) {
   t.tris = sc.tris;
   t.num_nodes = sc.num_nodes;
   t.extent = sc.extent;
+#ifdef LISA_BOUNDS
+  t.num_tris = sc.num_prims;
+#endif
   return t;
 }
 
@@ -300,6 +314,17 @@ template <bool COUNT>
 __device__ __forceinline__ NodeWork trav_node(TravState& s, const TraceScene& sc, uint2* stack, uint32_t& visits,
                                               uint32_t* status) {
   const RayPre& r = s.r;
+#ifdef LISA_BOUNDS
+  if (s.node >= sc.num_nodes) {  // end the ray
+    if (status) atomicOr(status, ST_BOUNDS);
+    NodeWork bad;
+    bad.tmask = 0;
+    bad.tri_base = 0;
+    bad.sp0 = 0;
+    s.sp = 0;
+    return bad;
+  }
+#endif
   if (COUNT) ++visits;
   const uint4* np = sc.nodes + 5ull * s.node;
   const uint4 n0 = __ldg(np + 0);
@@ -369,6 +394,12 @@ __device__ __forceinline__ NodeWork trav_node(TravState& s, const TraceScene& sc
     const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * (c & 3))) & 0xffu;
     w.tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
   }
+#ifdef LISA_BOUNDS
+  if (w.tmask && w.tri_base + (31u - (uint32_t)__clz(w.tmask)) >= sc.num_tris) {
+    if (status) atomicOr(status, ST_BOUNDS);
+    w.tmask = 0;
+  }
+#endif
   return w;
 }
 

@@ -71,6 +71,21 @@ __device__ __forceinline__ void warp_add64(unsigned long long* c, uint32_t v) {
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(c, (unsigned long long)v);
 }
 
+// Whether queue slot i, reserved by an append, lies inside the queue: always,
+// by construction (one entry per path and depth); checked in bounds-checked
+// builds, where a bad slot sets ST_QUEUE_OVERFLOW and the write is skipped.
+__device__ __forceinline__ bool queue_fits(const WaveBufs& b, uint32_t i) {
+#ifdef LISA_BOUNDS
+  if (i < b.capacity) return true;
+  atomicOr(&b.ctrl->status, ST_QUEUE_OVERFLOW);
+  return false;
+#else
+  (void)b;
+  (void)i;
+  return true;
+#endif
+}
+
 // The ray leaving a path's last vertex (physically based estimator) only
 // gathers emission: it is traced only if it may meet the scene's emitters.
 __device__ __forceinline__ bool final_ray_wanted(const SceneDev& sc, V3 p, V3 d) {
@@ -347,12 +362,12 @@ __global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
       }
     }
     const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
-    if (want_ray) {
+    if (want_ray && queue_fits(b, ri)) {
       b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
       b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
     }
     const uint32_t ni = warp_reserve(&b.ctrl->nee_count, want_nee);
-    if (want_nee) {
+    if (want_nee && queue_fits(b, ni)) {
       b.nee_a[ni] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
       b.nee_b[ni] = make_float4(N.x, N.y, N.z, __int_as_float(mat_idx));
       b.nee_c[ni] = make_float4(d.x, d.y, d.z, 0.0f);
@@ -457,7 +472,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
         }
       }
       const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
-      if (want_ray) {
+      if (want_ray && queue_fits(b, ri)) {
         b.ro[q ^ 1][ri] = make_float4(s.r.ox, s.r.oy, s.r.oz, __uint_as_float(slot));
         b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
       }
@@ -657,7 +672,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
         have = false;
       }
       const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
-      if (want_ray) {
+      if (want_ray && queue_fits(b, ri)) {
         b.ro[q ^ 1][ri] = make_float4(s.r.ox, s.r.oy, s.r.oz, __uint_as_float(slot));
         b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
       }
@@ -811,7 +826,7 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
       else want = guided_compat_vertex(b, depth, i, o, p, nd, slot, guided_n);
     }
     const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want);
-    if (want) {
+    if (want && queue_fits(b, ri)) {
       b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
       b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
     }

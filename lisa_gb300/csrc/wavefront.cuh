@@ -16,7 +16,7 @@ struct WaveBufs {
   uint32_t* ps_rng; // per slot: LCG state
   float4* nee_a;    // emitter-search queue: hit point xyz, w = slot
   float4* nee_b;    //                       shading normal xyz, w = material
-  float4* nee_c;    //                       incoming direction xyz, w = guide flag
+  float4* nee_c;    //                       incoming direction xyz, w unused
   WaveCtrl* ctrl;
   const SceneDev* scenes;
   uint32_t capacity;
