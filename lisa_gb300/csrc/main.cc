@@ -2,10 +2,13 @@
 // (src/LiSA/src/main.cc:6-27, src/LiSA/include/parse_args.hh:3-16):
 //
 //   lisa -s scene.rto [-d] [--guided] [--physical] [--seed N] [--reference-rng]
+//        [--autotune cache.json]
 //
 // -s   scene file (required)
 // -d   the reference's interactive display mode, headless: progressive
 //      launches of 16 spp until num_samples (render.cc:75-131), then the PPM
+// --autotune  queue and block sizes from the autotuner, kept in the given
+//      JSON cache (short probe renders the first time for a workload)
 // The image goes to the scene's output_image, as in render.cc:9-17.
 #include <chrono>
 #include <cstdio>
@@ -46,6 +49,13 @@ int main(int argc, char** argv) {
   if (has_option(argc, argv, "--physical")) opts.estimator = LISA_ESTIMATOR_PHYSICAL;
   if (has_option(argc, argv, "--reference-rng")) opts.rng = LISA_RNG_PER_PIXEL;
   if (const char* s = get_option(argc, argv, "--seed")) opts.seed = (uint32_t)std::strtoul(s, nullptr, 10);
+  if (const char* cache = get_option(argc, argv, "--autotune")) {
+    lisa_tuning t;
+    std::memset(&t, 0, sizeof(t));
+    t.struct_size = sizeof(t);
+    if (lisa_autotune(&params, 1, &opts, cache, &t) != LISA_OK) return fail("autotune");
+    lisa_tuning_apply(&t, &opts);
+  }
   lisa_renderer* r = nullptr;
   if (lisa_renderer_create(&params, &opts, &r) != LISA_OK) return fail("renderer");
   std::printf("Starting rendering...\n");
