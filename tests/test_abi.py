@@ -91,3 +91,17 @@ def test_ppm_writer_matches_save_image_layout(tmp_path):
     assert pix[1, 3, 1] == 3
     with pytest.raises(L.LisaError):
         L.write_ppm(str(tmp_path / "a.png"), rgba)
+
+
+def test_cli_reports_errors_like_the_reference_main(tmp_path):
+    """The `lisa` CLI (main.cc's interface): no -s prints the usage and
+    fails; a scene that does not exist fails with the parser's message,
+    before any device is touched."""
+    import os
+    import subprocess
+
+    cli = os.path.join(os.path.dirname(N.LIB_PATH), "bin", "lisa")
+    r = subprocess.run([cli], capture_output=True, text=True)
+    assert r.returncode == 1 and "Missing scene path" in r.stderr
+    r = subprocess.run([cli, "-s", str(tmp_path / "none.rto")], capture_output=True, text=True)
+    assert r.returncode == 1 and "not found" in r.stderr
