@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 def test_bounded_wait_runs_out_and_the_context_stays_usable(gpu):
     v = C.c_uint32(0)
-    N.check(N.lib().lisa_selftest_wait_timeout(1 << 12, C.byref(v)))
+    N.check(N.lib().lisa_selftest_wait_timeout(1 << 8, C.byref(v)))
     assert v.value & N.LISA_STATUS_WAIT_TIMEOUT
     sc = scenes.cornell_box(width=16, height=16, num_samples=1, num_bounces=2)
     r = L.Renderer(L.params_from_scene(sc))
