@@ -800,6 +800,18 @@ void* oracle_ctx_create(const oracle_scene* s, int use_bvh) {
 }
 void oracle_ctx_destroy(void* c) { delete (Ctx*)c; }
 
+// Closest hit of one ray (origin o, direction d) on [tmin, tmax] against a
+// scene context.  The host build of the reference's shader programs
+// (oracle/ref_shader_run.cc) calls it as its optixTrace.
+void oracle_ctx_closest(const void* ctx, const float* o, const float* d, float tmin, float tmax, int32_t* prim,
+                        float* t) {
+  int p;
+  float th;
+  closest(*(const Ctx*)ctx, v3(o[0], o[1], o[2]), v3(d[0], d[1], d[2]), tmin, tmax, &p, &th);
+  *prim = p;
+  *t = th;
+}
+
 int oracle_ctx_render(void* ctx, const oracle_scene* s, int threads, uint32_t px0, uint32_t px1, double* sum,
                       double* sumsq, uint64_t* rays);
 

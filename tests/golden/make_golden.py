@@ -13,12 +13,20 @@ Writes
                                      stderr message, parsed fields)
   tests/golden/ref_math.txt          reference math / BSDF / camera / tone
                                      map outputs on fixed inputs
+  tests/golden/shader/*.txt          per pixel, what the reference's own
+                                     shader programs (shader.cu run on the
+                                     host by oracle/_ref/ref_shader_run over
+                                     the reference parser's reading of the
+                                     scene) write: accumulation buffer, frame
+                                     buffer, trace counts.  Scenes:
+                                     tests/golden/shader_scenes.py
 """
 from __future__ import annotations
 
 import os
 import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -141,7 +149,31 @@ def main():
     r = subprocess.run([kdump], capture_output=True, text=True, check=True)
     with open(os.path.join(HERE, "ref_math.txt"), "w") as f:
         f.write(r.stdout)
-    print(f"wrote {len(CASES)} parser cases and ref_math.txt")
+    n = write_shader_fixtures()
+    print(f"wrote {len(CASES)} parser cases, ref_math.txt and {n} shader fixtures")
+
+
+def write_shader_fixtures() -> int:
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, HERE)
+    import shader_scenes
+    from lisa_gb300 import scenes
+
+    run = os.path.join(ROOT, "oracle", "_ref", "ref_shader_run")
+    out_dir = os.path.join(HERE, "shader")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, make in shader_scenes.SCENES.items():
+        sc = make()
+        with tempfile.TemporaryDirectory() as d:
+            rto = scenes.write_rto(sc, d)
+            r = subprocess.run([run, rto], capture_output=True, text=True, check=True)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith(("scene ", "px "))]
+        head = lines[0].split()
+        if head[8] != shader_scenes.soup_hash(sc):
+            sys.exit(f"{name}: the reference parser read another soup than the scene's")
+        with open(os.path.join(out_dir, name + ".txt"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+    return len(shader_scenes.SCENES)
 
 
 if __name__ == "__main__":

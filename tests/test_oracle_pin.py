@@ -154,3 +154,54 @@ def test_camera_frame_bit_exact(oracle):
         w, h = int(rec[7]), int(rec[8])
         L.oracle_uvw(ptr(eye), ptr(look), C.c_float(fov), w, h, ptr(out))
         assert np.array_equal(out, fa(rec[9:18]))
+
+
+# ---- the estimator loop against the reference's own shader programs ---------
+
+SHADER_DIR = os.path.join(HERE, "golden", "shader")
+
+
+def _shader_scenes():
+    import sys
+
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import shader_scenes
+
+    return shader_scenes
+
+
+@pytest.mark.parametrize("name", ["cornell", "hard_indirect", "rough_mix"])
+def test_estimator_matches_reference_shader(oracle, name):
+    """The oracle's estimator against the reference's shader.cu itself.
+
+    tests/golden/shader/<name>.txt holds, per pixel, what the reference's
+    raygen / closest-hit / miss programs (src/LiSA/src/shader.cu:102-255,
+    with lambertian.cu, maths.cu, random.h) wrote when run on the host over
+    the reference SceneParser's reading of the scene (one stream per pixel,
+    subframe 0, all spp in one launch as render.cc:133-148 does), with
+    closest hits from the oracle's scan.  The oracle in its per-pixel
+    stream mode must trace the same paths: the same number of radiance and
+    occlusion rays in every pixel (the reference also traces a ray of zero
+    direction, which the oracle counts as a miss without tracing it) and
+    the same mean.  The means may differ by rounding: the reference
+    accumulates samples in float and its BRDF and Schlick terms round
+    through double on the host; tolerance 1e-5 relative."""
+    S = _shader_scenes()
+    sc = S.SCENES[name]()
+    h, acc, _, cnt = S.read_fixture(os.path.join(SHADER_DIR, name + ".txt"))
+    assert h["soup"] == S.soup_hash(sc), "scene generator changed since the fixture was made"
+    assert (h["width"], h["height"], h["spp"], h["bounces"]) == (sc.width, sc.height, sc.num_samples,
+                                                                  sc.num_bounces)
+    osc = oracle.Scene.from_scene(sc, rng_mode=1, subframe=0)
+    npix = sc.width * sc.height
+    mean = np.empty((npix, 3), np.float32)
+    rays = np.empty((npix, 3), np.int64)
+    for p in range(npix):
+        s, _, r = osc.render(px0=p, px1=p + 1, threads=1)
+        mean[p] = s[0] / sc.num_samples
+        rays[p] = r.astype(np.int64)
+    assert np.array_equal(rays[:, 0] + rays[:, 1], cnt[:, 0] - cnt[:, 2]), "radiance rays differ"
+    assert np.array_equal(rays[:, 2], cnt[:, 1]), "occlusion rays differ"
+    assert np.all(np.abs(mean - acc) <= 1e-5 * np.maximum(1.0, np.abs(acc)))
+    assert (acc.sum(axis=1) > 0).sum() >= 20  # the scene is lit
+    assert cnt[:, 1].sum() > 10 * npix  # and the emitter search ran
