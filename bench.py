@@ -16,11 +16,15 @@ the data path; a barrier and a max-reduce of the time only).
 The line also carries `quality`: the equal-time relMSE of MLP-guided vs
 plain sampling on the hard-indirect scene (1024 x 1024, 256 spp, physically
 based estimator) against a 4,096-spp FP64 reference, measured in the same
-run after the timed region.
+run after the timed region; and `optix`: the reference's own OptiX render
+(baseline/optix_harness.cc, the reference's shader.cu and OptiX set-up) of
+the same workload on the same GPU, 16 spp per launch.
 
---impl reference times the reference estimator's CPU restatement (the
-oracle: LiSA's own GPU path is OptiX and does not build here) on all host
-cores, on a bounded sample of the same workload.
+--impl reference times the reference's own estimator code on the host
+cores: src/LiSA/src/shader.cu compiled for the CPU (oracle/ref_shader_run.cc,
+closest hits from the oracle's CPU BVH) on all host threads, on a bounded
+sample of the same workload; where it was not built, the oracle's
+restatement of it.  --impl optix prints the OptiX render's own line.
 """
 from __future__ import annotations
 
@@ -206,24 +210,103 @@ def cpu_sample(scene, spp, budget_s=12.0, threads=0, seed=0):
             f"{px_tot} pixels in {bands} bands x {spp} spp of the same frame (CPU BVH built once, not timed)", cores)
 
 
+REF_SHADER = os.path.join(ROOT, "oracle", "_ref", "ref_shader_run")
+
+
+class RefShaderSample:
+    """The reference's own estimator (shader.cu compiled for the host,
+    oracle/ref_shader_run.cc) timed on a sample of the workload: 64 rows
+    spread over the frame, 64 pixels of each, on all host threads.  The scene
+    is written once as a raw soup; the CPU BVH is built outside the timed
+    region."""
+
+    def __init__(self, scene, rows=64, band=64, threads=0):
+        import tempfile
+
+        sys.path.insert(0, os.path.join(ROOT, "baseline"))
+        import optix_run
+
+        self.dir = tempfile.TemporaryDirectory()
+        self.path = os.path.join(self.dir.name, "scene.soup")
+        optix_run.write_soup(scene, self.path)
+        self.rows, self.band, self.threads = rows, band, threads
+
+    def __call__(self, spp):
+        cmd = [REF_SHADER, "--soup", self.path, "--spp", str(spp), "--rows", str(self.rows), "--band",
+               str(self.band)]
+        if self.threads:
+            cmd += ["--threads", str(self.threads)]
+        d = json.loads(subprocess.run(cmd, capture_output=True, text=True, check=True).stdout.strip().splitlines()[-1])
+        rays = d["rays_radiance"] + d["rays_occlusion"]
+        desc = (f"{d['pixels']} pixels ({self.rows} rows x {self.band}) x {spp} spp of the same frame; the "
+                f"reference's shader.cu compiled for the host, every trace counted (CPU BVH built once, not timed)")
+        return rays / d["seconds"] / 1e6, desc, d["threads"]
+
+
+def cpu_reference(scene, spp, steps=1, seed=0, budget_s=12.0):
+    """(Mrays/s per step, description, cores, kind) of the CPU baseline:
+    the reference's own estimator code where it was built, else the oracle's
+    restatement."""
+    if os.path.exists(REF_SHADER):
+        run = RefShaderSample(scene)
+        out = [run(spp) for _ in range(steps)]
+        return [o[0] for o in out], out[-1][1], out[-1][2], "reference"
+    vals = []
+    for i in range(steps):
+        v, desc, cores = cpu_sample(scene, spp=spp, budget_s=budget_s, seed=seed + i)
+        vals.append(v)
+    return vals, desc, cores, "port"
+
+
+def optix_reference(scene, spp, warmup=2, reps=5):
+    """The reference's OptiX render of `scene` on this GPU
+    (baseline/optix_harness.cc), or {"unavailable": why}."""
+    sys.path.insert(0, os.path.join(ROOT, "baseline"))
+    import optix_run
+
+    why = optix_run.available()
+    if why:
+        return {"unavailable": why}
+    try:
+        r = optix_run.run(scene, spp=spp, warmup=warmup, reps=reps, count=True)
+    except Exception as e:  # noqa: BLE001 - reported, not fatal to our own line
+        return {"unavailable": f"OptiX harness failed: {str(e)[-300:]}"}
+    return {"value": r["mrays_per_s"], "unit": "Mrays/s", "ms_per_launch": r["ms_per_launch"],
+            "rays_per_launch": r["rays"], "rays_radiance": r["rays_radiance"], "rays_occlusion": r["rays_occlusion"],
+            "spp_per_launch": r["spp"], "launches_timed": r["reps"],
+            "what": "the reference's own OptiX pipeline (optix_wrapper.cc set-up, shader.cu compiled with its "
+                    "--use_fast_math flags), one optixLaunch of width x height per step, CUDA events on its "
+                    "stream; rays counted by an instrumented copy of shader.cu in a separate untimed launch"}
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
         return
     sc = make_scene(res=args.res)
-    vals = []
-    desc, cores = "", os.cpu_count()
-    for i in range(args.warmup + args.steps):
-        v, desc, cores = cpu_sample(sc, spp=args.spp_per_step, budget_s=args.ref_budget, seed=i)
-        if i >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
+    vals, desc, cores, kind = cpu_reference(sc, args.spp_per_step, steps=args.warmup + args.steps,
+                                            budget_s=args.ref_budget)
+    value = float(np.mean(vals[args.warmup:]))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "l2": "host-side run"},
-            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
-                             "sample": desc},
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": kind, "sample": desc},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_optix(args, rank, ws):
+    if rank != 0:
+        return
+    sc = make_scene(res=args.res)
+    o = optix_reference(sc, args.spp_per_step, warmup=args.warmup, reps=args.steps)
+    if "unavailable" in o:
+        print(json.dumps({"impl": "optix", "unavailable": o["unavailable"]}), flush=True)
+        return
+    line = {"impl": "optix", "metric": METRIC, "value": o["value"], "unit": "Mrays/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": o["ms_per_launch"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD}, "optix": o}
     print(json.dumps(line), flush=True)
 
 
@@ -338,8 +421,13 @@ def run_ours(args, rank, ws, local):
                    "guided_time_to_plain_error": q["time_to_plain_error"]}
     cpu = None
     if rank == 0 and not (args.no_cpu or args.quick):
-        cv, cdesc, ccores = cpu_sample(sc, spp=args.spp_per_step, budget_s=args.cpu_budget)
-        cpu = {"value": cv, "unit": "Mrays/s", "cores": ccores, "kind": "port", "sample": cdesc}
+        cv, cdesc, ccores, ckind = cpu_reference(sc, args.spp_per_step, steps=1, budget_s=args.cpu_budget)
+        cpu = {"value": cv[0], "unit": "Mrays/s", "cores": ccores, "kind": ckind, "sample": cdesc}
+    optix = None
+    if rank == 0 and not (args.quick or args.no_optix):
+        optix = optix_reference(sc, args.spp_per_step)
+        if "value" in optix:
+            optix["plain_over_optix"] = value / optix["value"]
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -376,6 +464,7 @@ def run_ours(args, rank, ws, local):
             "clocks": clocks,
             "gpu_launches": int(launches),
             "quality": quality,
+            "optix": optix,
         }
         print(json.dumps(line), flush=True)
 
@@ -385,7 +474,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "optix"])
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--paths", type=int, default=0, help="paths in flight (0 = library default)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -394,6 +483,7 @@ def main():
     ap.add_argument("--res", type=int, default=1024, help="square resolution (profiling cases use less)")
     ap.add_argument("--quick", action="store_true", help="skip the CPU baseline, the end-to-end leg and the quality leg")
     ap.add_argument("--no-quality", action="store_true", help="skip the guided-vs-plain relMSE leg")
+    ap.add_argument("--no-optix", action="store_true", help="skip the reference's OptiX render leg")
     ap.add_argument("--no-tune", action="store_true", help="library default queue and block sizes")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -401,6 +491,8 @@ def main():
     rank, ws, local = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, ws)
+    elif args.impl == "optix":
+        run_optix(args, rank, ws)
     else:
         run_ours(args, rank, ws, local)
     if ws > 1:

@@ -43,11 +43,16 @@
 // raygen program wrote (float bits), the frame buffer bytes, and the number
 // of radiance traces, occlusion traces and radiance traces with a zero
 // direction that the pixel made.
+// With --soup (a raw soup, no text parsing) it times the raygen over a
+// sample of pixels on all host threads instead: the reference's own
+// estimator as a CPU baseline (closest hits from the oracle's CPU BVH).
 #include <omp.h>
 
 #include <cstdint>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "scene_parser.hh"
@@ -199,13 +204,92 @@ static uint32_t bits(float f) {
   return u;
 }
 
+// A raw soup (the arrays SceneParser produces, without text parsing), in the
+// format baseline/optix_harness.cc reads: magic "LSOUP1\0\0", u32 T, M,
+// width, height, spp, bounces; f32 eye[3], look_at[3], fov; f32
+// vertices[9T], normals[9T]; i32 mat_indices[T]; Material[M] (40 bytes).
+struct Soup {
+  std::vector<float3> vertices, normals;
+  std::vector<int> mat_indices;
+  std::vector<Material> materials;
+};
+
+static bool load_soup(const char* path, Soup& s, RendererParams& p) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  char magic[8];
+  uint32_t h[6];
+  float cam[7];
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "LSOUP1", 6) == 0 &&
+            std::fread(h, 4, 6, f) == 6 && std::fread(cam, 4, 7, f) == 7;
+  if (ok) {
+    const size_t T = h[0], M = h[1];
+    s.vertices.resize(3 * T);
+    s.normals.resize(3 * T);
+    s.mat_indices.resize(T);
+    s.materials.resize(M);
+    ok = std::fread(s.vertices.data(), sizeof(float3), 3 * T, f) == 3 * T &&
+         std::fread(s.normals.data(), sizeof(float3), 3 * T, f) == 3 * T &&
+         std::fread(s.mat_indices.data(), sizeof(int), T, f) == T &&
+         std::fread(s.materials.data(), sizeof(Material), M, f) == M;
+    p.vertices = s.vertices.data();
+    p.normals = s.normals.data();
+    p.materials = s.materials.data();
+    p.mat_indices = s.mat_indices.data();
+    p.num_vertices = (int)(3 * T);
+    p.num_materials = (int)M;
+    p.width = h[2];
+    p.height = h[3];
+    p.num_samples = h[4];
+    p.num_bounces = h[5];
+    p.camera.eye = make_float3(cam[0], cam[1], cam[2]);
+    p.camera.look_at = make_float3(cam[3], cam[4], cam[5]);
+    p.camera.fov = cam[6];
+    p.output_image = "";
+  }
+  std::fclose(f);
+  return ok;
+}
+
 int main(int argc, char** argv) {
-  if (argc < 2) {
-    std::fprintf(stderr, "usage: %s scene.rto\n", argv[0]);
+  // ref_shader_run scene.rto                  per-pixel dump of the whole frame
+  // ref_shader_run --soup scene.soup --spp N --rows R --band K [--threads T]
+  //     times the reference's raygen over a sample of the frame: R rows
+  //     spread evenly over the image, K pixels of each (starting at
+  //     (row index * 97) mod (width - K)), N samples per pixel; prints one
+  //     JSON line with the traces made and the seconds taken.
+  const char* rto = nullptr;
+  const char* soup_path = nullptr;
+  int spp = -1, rows = 0, band = 0, threads = 0;
+  for (int i = 1; i < argc; ++i) {
+    const std::string a = argv[i];
+    if (a == "--soup" && i + 1 < argc) soup_path = argv[++i];
+    else if (a == "--spp" && i + 1 < argc) spp = std::atoi(argv[++i]);
+    else if (a == "--rows" && i + 1 < argc) rows = std::atoi(argv[++i]);
+    else if (a == "--band" && i + 1 < argc) band = std::atoi(argv[++i]);
+    else if (a == "--threads" && i + 1 < argc) threads = std::atoi(argv[++i]);
+    else if (a[0] != '-' && !rto) rto = argv[i];
+    else {
+      std::fprintf(stderr, "usage: %s scene.rto | --soup f --spp N --rows R --band K [--threads T]\n", argv[0]);
+      return 2;
+    }
+  }
+  if (!rto == !soup_path) {
+    std::fprintf(stderr, "usage: %s scene.rto | --soup f --spp N --rows R --band K [--threads T]\n", argv[0]);
     return 2;
   }
-  SceneParser parser(argv[1]);
-  const RendererParams rp = parser.get_params();
+  Soup soup;
+  SceneParser* parser = nullptr;
+  RendererParams rp{};
+  if (rto) {
+    parser = new SceneParser(const_cast<char*>(rto));
+    rp = parser->get_params();
+  } else if (!load_soup(soup_path, soup, rp)) {
+    std::fprintf(stderr, "cannot read soup %s\n", soup_path);
+    return 1;
+  }
+  if (spp > 0) rp.num_samples = (unsigned)spp;
+  if (threads > 0) omp_set_num_threads(threads);
   const uint32_t T = (uint32_t)rp.num_vertices / 3u;
 
   OracleScene os;
@@ -247,6 +331,36 @@ int main(int argc, char** argv) {
   params.eye = cam.eye();
   cam.UVWFrame(params.U, params.V, params.W);
 
+  if (soup_path) {
+    // timed sample: the pixels of R rows x K columns
+    std::vector<int64_t> pix;
+    const int w = (int)rp.width, h = (int)rp.height;
+    const int R = rows > 0 ? rows : 64, K = band > 0 ? std::min(band, w) : std::min(64, w);
+    for (int b = 0; b < R; ++b) {
+      const int y = R > 1 ? (int)((double)b * (h - 1) / (R - 1)) : 0;
+      const int x0 = w > K ? (b * 97) % (w - K) : 0;
+      for (int k = 0; k < K; ++k) pix.push_back((int64_t)y * w + x0 + k);
+    }
+    uint64_t rad = 0, occ = 0, zero = 0;
+    const double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : rad, occ, zero)
+    for (int64_t i = 0; i < (int64_t)pix.size(); ++i) {
+      const int64_t p = pix[i];
+      t_launch = make_uint3((unsigned)(p % rp.width), (unsigned)(p / rp.width), 0u);
+      t_counts = Counts{};
+      __raygen__rg();
+      rad += t_counts.radiance;
+      occ += t_counts.occlusion;
+      zero += t_counts.zero_dir;
+    }
+    const double sec = omp_get_wtime() - t0;
+    std::printf("{\"pixels\": %zu, \"spp\": %u, \"seconds\": %.6f, \"rays_radiance\": %llu, \"rays_occlusion\": "
+                "%llu, \"rays_zero_direction\": %llu, \"threads\": %d}\n",
+                pix.size(), rp.num_samples, sec, (unsigned long long)rad, (unsigned long long)occ,
+                (unsigned long long)zero, omp_get_max_threads());
+    return 0;
+  }
+
   const int64_t npix = (int64_t)rp.width * rp.height;
   std::vector<Counts> counts(npix);
 #pragma omp parallel for schedule(dynamic, 4)
@@ -270,5 +384,6 @@ int main(int argc, char** argv) {
                 bits(a.z), c.x, c.y, c.z, c.w, (unsigned long long)counts[p].radiance,
                 (unsigned long long)counts[p].occlusion, (unsigned long long)counts[p].zero_dir);
   }
+  delete parser;
   return 0;
 }

@@ -221,3 +221,9 @@ def test_matches_reference_shader_fixture(gpu, tmp_path, name):
     assert st.rays_primary + st.rays_bounce == int((cnt[:, 0] - cnt[:, 2]).sum())
     assert st.rays_shadow == int(cnt[:, 1].sum())
     assert st.device_status == 0
+    # the reference's own OptiX render of the scene with closest-hit
+    # occlusion rays (tests/golden/optix): the same paths except where
+    # OptiX's triangle intersector rounds a hit distance differently
+    optix = np.fromfile(os.path.join(here, "golden", "optix", name + "_closest.f32"), np.float32).reshape(-1, 3)
+    same = (np.abs(optix - img) <= 1e-5 * np.maximum(1.0, np.abs(img))).all(axis=1)
+    assert same.mean() >= 0.90, same.mean()
