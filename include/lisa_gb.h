@@ -280,16 +280,18 @@ int lisa_trace_brute_device(lisa_renderer* r, const float* d_rays, uint32_t n, i
 /* Closest hit of num_rays device rays (same layout and tie rule as
  * lisa_trace_closest) against a soup of num_triangles triangles given as
  * device vertices (9 floats per triangle), with no device allocation: the
- * BVH is built in a scratch array compiled into the library (about 17 MB,
- * held on every GPU that loads it).  No counterpart in the reference; it
+ * BVH is built in a scratch array compiled into the library (21 MiB =
+ * 22,020,096 bytes, held on every GPU that loads it).  No counterpart in the reference; it
  * serves callers that cannot call cudaMalloc/cudaFree at query time (a
  * plugin inside an application whose allocator owns the device memory, or
  * a per-frame loop that cannot take cudaFree's device-wide sync).  Limits
  * and contract: at most 65536 triangles (larger soups return
- * LISA_ERR_INVALID); the first call on a device looks up the scratch
- * address and should come before any stream capture; calls share the
- * scratch, so calls that overlap on the GPU race and must be serialised by
- * the caller.  Synchronises `stream` (cudaStream_t, NULL = default). */
+ * LISA_ERR_INVALID); the first call in a CUDA context looks up the
+ * scratch address (cached per context) and should come before any stream
+ * capture; calls share the scratch, so calls that overlap on the GPU race
+ * and must be serialised by the caller.  num_rays == 0 returns at once
+ * without touching the scratch or the stream; otherwise the call
+ * synchronises `stream` (cudaStream_t, NULL = default). */
 int lisa_trace_soup_noalloc(const float* d_vertices, uint32_t num_triangles, const float* d_rays,
                             uint32_t num_rays, int32_t* d_prim, float* d_t, void* stream);
 /* Node visits and triangle tests of the last counted traversal pass:

@@ -11,15 +11,21 @@
 // into the caller's output buffers.
 //
 // The scratch is the file-scope array below.  Every GPU that loads the
-// library holds it (NOALLOC_SCRATCH_BYTES, about 17 MB) until the process
-// exits.  Its host-side name is only a stand-in for the device array, so
-// host code obtains the device address with cudaGetSymbolAddress, once per
-// device, the first time the entry point runs on that device (with that
-// device current); that first call should therefore come before any stream
-// capture.  All calls share the one array and it keeps the previous call's
-// contents: every counter the build needs zeroed is cleared at the start of
-// each call, and calls that overlap on the GPU (two host threads, or two
-// streams) race on the array, so callers must serialise them.
+// library holds it (NOALLOC_SCRATCH_BYTES = 22,020,096 bytes, 21 MiB) until
+// the process exits.  Its host-side name is only a stand-in for the device
+// array, so host code obtains the device address with cudaGetSymbolAddress,
+// once per CUDA context, the first time the entry point runs in that
+// context (with it current); that first call should therefore come before
+// any stream capture.  The address belongs to the context the module was
+// loaded into, so it is cached by the context's unique ID (cuCtxGetId): a
+// caller that makes its own context current, or a cudaDeviceReset that
+// replaces the primary context, gets a fresh look-up.  All calls share the
+// one array and it keeps the previous call's contents: every counter the
+// build needs zeroed is cleared at the start of each call, and calls that
+// overlap on the GPU (two host threads, or two streams) race on the array,
+// so callers must serialise them.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -39,25 +45,73 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)NOALLOC_MAX_TRIANGLES * 320 + (
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-constexpr int MAX_DEVICES = 64;
+// Scratch addresses already looked up, by CUDA context ID.  Contexts are
+// few (one primary context per device, plus any a host application creates);
+// the table is a small ring, a full one re-uses its oldest slot.
+constexpr int MAX_CONTEXTS = 64;
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  void* ptr;
+};
 std::mutex g_mu;
-void* g_scratch_ptr[MAX_DEVICES] = {};
+ScratchEntry g_scratch[MAX_CONTEXTS] = {};
+int g_scratch_used = 0, g_scratch_next = 0;
 
-// Device address of the scratch array on the current device (set up once
-// per device).
-Status scratch_address(int dev, void** out) {
-  if (dev < 0 || dev >= MAX_DEVICES) return Status::invalid("device index out of range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return Status::cuda(e, "cudaGetSymbolAddress(no-allocation scratch)");
-    }
-    g_scratch_ptr[dev] = p;
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique ID of the current CUDA context (the driver API through the
+// runtime's entry-point query, so the library needs no libcuda link).
+// *none is set when no context is current yet.
+Status current_context_id(unsigned long long* id, bool* none) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    LISA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+    LISA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return Status(LISA_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
+    get_current = (PfnCtxGetCurrent)f1;
+    get_id = (PfnCtxGetId)f2;
   }
-  *out = g_scratch_ptr[dev];
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return Status(LISA_ERR_CUDA, "cuCtxGetCurrent failed");
+  *none = ctx == nullptr;
+  if (*none) return Status();
+  if (get_id(ctx, id) != CUDA_SUCCESS) return Status(LISA_ERR_CUDA, "cuCtxGetId failed");
+  return Status();
+}
+
+// Device address of the scratch array in the current context (looked up
+// once per context).
+Status scratch_address(void** out) {
+  unsigned long long id = 0;
+  bool none = false;
+  LISA_TRY(current_context_id(&id, &none));
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!none)
+    for (int i = 0; i < g_scratch_used; ++i)
+      if (g_scratch[i].ctx_id == id) {
+        *out = g_scratch[i].ptr;
+        return Status();
+      }
+  // with no context current, this binds the device's primary context
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return Status::cuda(e, "cudaGetSymbolAddress(no-allocation scratch)");
+  }
+  if (none) {
+    LISA_TRY(current_context_id(&id, &none));
+    if (none) return Status(LISA_ERR_CUDA, "no CUDA context after the scratch look-up");
+  }
+  const int slot = g_scratch_used < MAX_CONTEXTS ? g_scratch_used++ : (g_scratch_next++ % MAX_CONTEXTS);
+  g_scratch[slot] = ScratchEntry{id, p};
+  *out = p;
   return Status();
 }
 
@@ -68,12 +122,14 @@ Status trace_soup_noalloc(const float* d_vertices, uint32_t num_triangles, const
                            " exceeds the no-allocation limit of " + std::to_string(NOALLOC_MAX_TRIANGLES));
   if ((num_triangles && !d_vertices) || (num_rays && (!d_rays || !d_prim || !d_t)))
     return Status::invalid("null buffer");
+  // nothing to trace: touch neither the scratch nor the stream
+  if (num_rays == 0) return Status();
   int dev = 0;
   LISA_CUDA(cudaGetDevice(&dev));
   int sm = 0;
   LISA_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev));
   void* base = nullptr;
-  LISA_TRY(scratch_address(dev, &base));
+  LISA_TRY(scratch_address(&base));
   BumpScratch region(base, NOALLOC_SCRATCH_BYTES);
   SceneDev* d_scene = nullptr;
   WaveCtrl* d_ctrl = nullptr;

@@ -28,10 +28,10 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def _reference_hits(sc, rays_d, n):
+def _reference_hits(sc, rays_d, n, params=None):
     import torch
 
-    r = L.Renderer(L.params_from_scene(sc, num_samples=1))
+    r = L.Renderer(params if params is not None else L.params_from_scene(sc, num_samples=1))
     prim = torch.empty(n, dtype=torch.int32, device="cuda")
     t = torch.empty(n, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
@@ -69,6 +69,45 @@ def test_noalloc_matches_renderer_trace_on_consecutive_calls(gpu):
         assert hit.mean() > 0.3
         assert np.array_equal(got_t[hit].view(np.uint32), ref_t[hit].view(np.uint32))
         assert np.all(np.isinf(got_t[~hit]))
+
+
+@pytest.mark.gpu
+def test_noalloc_at_the_triangle_limit(gpu):
+    """A soup of exactly 65,536 triangles (the limit) fits the scratch and
+    gives the renderer's hits bit for bit."""
+    sc = scenes.icosphere_box(level=6)  # 81,932 triangles, cut to the limit
+    v, n, mi = sc.soup()
+    T = 65536
+    v, n, mi = v[:3 * T], n[:3 * T], mi[:T]
+    params = L.params_from_arrays(v, n, mi, sc.material_table(), 64, 64, sc.eye, sc.look_at, sc.fov, 1, 2)
+    rays = random_rays(v, 100_000, seed=31, eye=sc.eye)
+    rays_d = _dev(rays)
+    got_p, got_t = _noalloc_hits(_dev(v.reshape(-1)), T, rays_d, rays.shape[0])
+    ref_p, ref_t = _reference_hits(sc, rays_d, rays.shape[0], params=params)
+    assert np.array_equal(got_p, ref_p)
+    hit = ref_p >= 0
+    assert hit.mean() > 0.3
+    assert np.array_equal(got_t[hit].view(np.uint32), ref_t[hit].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_noalloc_empty_soup_and_no_rays(gpu):
+    """No triangles: every ray misses (prim -1, t = inf).  No rays: the
+    call succeeds and writes nothing."""
+    import torch
+
+    rays = random_rays(scenes.cornell_box().soup()[0], 1000, seed=5)
+    rays_d = _dev(rays)
+    dummy = torch.zeros(9, dtype=torch.float32, device="cuda")
+    got_p, got_t = _noalloc_hits(dummy, 0, rays_d, rays.shape[0])
+    assert np.all(got_p == -1) and np.all(np.isinf(got_t))
+    prim = torch.full((4,), -7, dtype=torch.int32, device="cuda")
+    t = torch.zeros(4, dtype=torch.float32, device="cuda")
+    p = C.c_void_p
+    N.check(N.lib().lisa_trace_soup_noalloc(p(dummy.data_ptr()), 1, p(rays_d.data_ptr()), 0, p(prim.data_ptr()),
+                                            p(t.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert np.all(prim.cpu().numpy() == -7)
 
 
 @pytest.mark.gpu
