@@ -141,6 +141,41 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def measured_peak_bf16(sustained=True):
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops_sustained" if sustained else "bf16_tflops"]), "of measured"
+    except (OSError, KeyError, ValueError):
+        return (1700.0 if sustained else 1900.0), "of fallback"
+
+
+# guide network FLOPs per sample (N = 40 outputs, unpadded): forward
+# 2*(4*64*64 + 64*40); a training sample runs the forward pass and the
+# backward pass (twice the forward's products)
+MLP_FWD_FLOP = 2 * (4 * 64 * 64 + 64 * 40)
+MLP_TRAIN_FLOP = 3 * MLP_FWD_FLOP
+
+
+def mlp_roofline(guided_row):
+    """Tensor-pipe roofline of the guide's kernels inside the guided render:
+    inference (k_guided_infer: the network on every emitter-queue entry of a
+    guided depth, fused with the guided bounce) and training (sample
+    collection, k_guide_train, Adam), from the renderer's stage timers and
+    its work counters, against the sustained bf16 peak (the kernels run
+    inside a long render)."""
+    peak, kind = measured_peak_bf16(sustained=True)
+    out = {}
+    for key, unit_key, flop in (("guide_infer", "rows", MLP_FWD_FLOP), ("guide_train", "samples", MLP_TRAIN_FLOP)):
+        g = guided_row.get(key) or {}
+        ms, units = g.get("ms", 0.0), g.get(unit_key, 0)
+        tf = units * flop / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
+        out[key] = {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+                    "peak_kind": kind, unit_key: units, "ms": ms, "flop_per_unit": flop}
+    return out
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -277,6 +312,48 @@ def optix_reference(scene, spp, warmup=2, reps=5):
             "what": "the reference's own OptiX pipeline (optix_wrapper.cc set-up, shader.cu compiled with its "
                     "--use_fast_math flags), one optixLaunch of width x height per step, CUDA events on its "
                     "stream; rays counted by an instrumented copy of shader.cu in a separate untimed launch"}
+
+
+def soup_leg(args, local, spp=4, steps=3):
+    """The triangle-soup stress workload: 20,000 UV spheres of 16 x 8
+    segments (224 triangles each: the pole rows are triangles; 4,480,000 in
+    all), 10 % emissive, in a 100^3 box; 1920 x 1080, 12 bounces, reference
+    estimator; `spp` samples per step, L2 flushed before each step.  Also the
+    reference's OptiX render of the same scene where it runs."""
+    import torch
+
+    import lisa_gb300 as L
+    from lisa_gb300 import scenes
+
+    sc = scenes.sphere_soup()
+    r = L.Renderer(L.params_from_scene(sc), L.default_options(stage_timing=1))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    stats = []
+    for i in range(steps + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = r.render_progressive(spp)
+        if i:
+            stats.append(st)
+    ms = sum(s.ms_device for s in stats) / len(stats)
+    rays = sum(s.rays for s in stats) / len(stats)
+    out = {"workload": "20,000 UV spheres 16x8 (224 tris each, 4,480,000 tris, 20,000 materials, 10% emissive) in a "
+                       "100^3 box, 1920x1080, 12 bounces, compat estimator",
+           "spp_per_step": spp, "steps": steps, "value": rays / ms / 1e3, "unit": "Mrays/s", "ms_per_step": ms,
+           "rays_per_step": rays,
+           "shadow_traversals_per_step": sum(s.shadow_traversals for s in stats) / len(stats),
+           "stages_ms_per_step": {"trace": sum(s.ms_trace for s in stats) / len(stats),
+                                  "shade": sum(s.ms_shade for s in stats) / len(stats),
+                                  "nee": sum(s.ms_nee for s in stats) / len(stats)},
+           "bvh": r.bvh_info()}
+    r.close()
+    del flush
+    if not args.no_optix:
+        o = optix_reference(sc, spp, warmup=1, reps=steps)
+        out["optix"] = o
+        if "ms_per_launch" in o:
+            out["optix"]["time_over_ours"] = o["ms_per_launch"] / ms
+    return out
 
 
 def run_reference(args, rank, ws):
@@ -418,7 +495,11 @@ def run_ours(args, rank, ws, local):
                    "relmse_plain": q["plain"]["relmse_corrected"], "relmse_guided": q["guided"]["relmse_corrected"],
                    "ms_plain": q["plain"]["ms"], "ms_guided": q["guided"]["ms"],
                    "equal_time_relmse_guided_over_plain": q["equal_time_relmse"]["guided"] / q["equal_time_relmse"]["plain"],
-                   "guided_time_to_plain_error": q["time_to_plain_error"]}
+                   "guided_time_to_plain_error": q["time_to_plain_error"],
+                   "mlp": mlp_roofline(q["guided"])}
+    soup = None
+    if rank == 0 and not (args.quick or args.no_soup):
+        soup = soup_leg(args, local)
     cpu = None
     if rank == 0 and not (args.no_cpu or args.quick):
         cv, cdesc, ccores, ckind = cpu_reference(sc, args.spp_per_step, steps=1, budget_s=args.cpu_budget)
@@ -465,6 +546,7 @@ def run_ours(args, rank, ws, local):
             "gpu_launches": int(launches),
             "quality": quality,
             "optix": optix,
+            "soup": soup,
         }
         print(json.dumps(line), flush=True)
 
@@ -484,6 +566,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the CPU baseline, the end-to-end leg and the quality leg")
     ap.add_argument("--no-quality", action="store_true", help="skip the guided-vs-plain relMSE leg")
     ap.add_argument("--no-optix", action="store_true", help="skip the reference's OptiX render leg")
+    ap.add_argument("--no-soup", action="store_true", help="skip the triangle-soup stress leg")
     ap.add_argument("--no-tune", action="store_true", help="library default queue and block sizes")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -171,6 +171,15 @@ typedef struct lisa_render_stats {
   uint64_t tri_tests_trace;
   uint64_t node_visits_nee;
   uint64_t tri_tests_nee;
+  uint64_t shadow_traversals;  /* emitter-search rays that walked the BVH; the
+                                * rest of rays_shadow could neither light their
+                                * vertex nor change its emitter flag (they
+                                * cannot reach an emitter and the flag was
+                                * unset), so only their count was kept      */
+  double ms_guide_infer;       /* guide stage split (stage_timing): inference */
+  double ms_guide_train;       /* and training (collection, steps, Adam)      */
+  uint64_t guide_infer_rows;   /* emitter-queue entries the inference ran on  */
+  uint64_t guide_train_samples;/* samples of the training steps               */
 } lisa_render_stats;
 
 typedef struct lisa_scene lisa_scene;

@@ -83,7 +83,10 @@ class RenderStats(C.Structure):
                 ("launches_total", C.c_uint32), ("device_status", C.c_uint32),
                 ("guide_loss", C.c_double), ("nee_vertices", C.c_uint64),
                 ("node_visits_trace", C.c_uint64), ("tri_tests_trace", C.c_uint64),
-                ("node_visits_nee", C.c_uint64), ("tri_tests_nee", C.c_uint64)]
+                ("node_visits_nee", C.c_uint64), ("tri_tests_nee", C.c_uint64),
+                ("shadow_traversals", C.c_uint64), ("ms_guide_infer", C.c_double),
+                ("ms_guide_train", C.c_double), ("guide_infer_rows", C.c_uint64),
+                ("guide_train_samples", C.c_uint64)]
 
     @property
     def rays(self) -> int:

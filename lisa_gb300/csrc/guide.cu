@@ -194,7 +194,8 @@ template <int SRC>
 __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restrict__ pack, const float* __restrict__ master,
                                                         GuideSrc src, float inv_n, float* __restrict__ part,
                                                         float* __restrict__ loss_part, uint32_t* status,
-                                                        uint32_t* __restrict__ step_bump) {
+                                                        uint32_t* __restrict__ step_bump,
+                                                        unsigned long long* __restrict__ sample_count) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
@@ -214,6 +215,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   const uint32_t ntiles = (n - src.first + 127) / 128;
   // the Adam step that follows (none for an empty slice)
   if (step_bump && n > src.first && blockIdx.x == 0 && threadIdx.x == 0) *step_bump += 1;
+  if (sample_count && n > src.first && blockIdx.x == 0 && threadIdx.x == 0) *sample_count += n - src.first;
   float* slot = part + (size_t)blockIdx.x * NPARAM;  // this CTA's partial gradient
   if (blockIdx.x >= ntiles) {
     for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) slot[k] = 0.0f;
@@ -525,7 +527,7 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
 // step (or guide_launch_reduce) sums them.  With adam_follows the device
 // step count advances for the Adam step launched next.
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s, bool adam_follows) {
+                          cudaStream_t s, bool adam_follows, unsigned long long* sample_count) {
   if (!g.grad_part) return Status::invalid("guide: no partial-gradient slots");
   const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
   const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
@@ -533,10 +535,10 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float 
   uint32_t* bump = adam_follows ? g.d_step : nullptr;
   if (src_kind == SRC_RAW)
     k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
-                                                         g.status, bump);
+                                                         g.status, bump, sample_count);
   else
     k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
-                                                          g.status, bump);
+                                                          g.status, bump, sample_count);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }

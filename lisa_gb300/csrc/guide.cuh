@@ -67,9 +67,9 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
                           cudaStream_t s);
 // one training launch: each CTA writes its partial gradient and loss to its
 // slot; with adam_follows the device step count advances for the next Adam
-// step
+// step; sample_count (optional) accumulates the samples trained on
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s, bool adam_follows);
+                          cudaStream_t s, bool adam_follows, unsigned long long* sample_count = nullptr);
 // g.grads / g.loss = sums of the last training launch's partials
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s);
 // Adam step on the summed partials; also refreshes the BF16 weights and

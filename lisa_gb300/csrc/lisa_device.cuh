@@ -133,6 +133,9 @@ struct WaveCtrl {
   unsigned long long node_visits[2];  // [0] closest-hit stage, [1] emitter search
   unsigned long long tri_tests[2];
   unsigned long long nee_total;
+  unsigned long long shadow_walked;   // emitter-search rays that walked the BVH
+  unsigned long long infer_rows;      // emitter-queue entries the guide's inference ran on
+  unsigned long long train_samples;   // samples of the guide's training steps
 };
 
 // ---------------------------------------------------------------------------
@@ -540,6 +543,23 @@ __device__ __forceinline__ bool box_may_hit(const RayPre& r, const float* lo, co
   const float tn = fmaxf(fmaxf(fminf(ax, bx) - gx, fminf(ay, by) - gy), fmaxf(fminf(az, bz) - gz, tmin));
   const float tf = fminf(fminf(fmaxf(ax, bx) + gx, fmaxf(ay, by) + gy), fminf(fmaxf(az, bz) + gz, tmax));
   return tn <= tf;
+}
+
+// Whether a ray from o along d may meet the scene's emissive triangles
+// inside (RAY_TMIN, RAY_TMAX): box_may_hit against their padded bounds with
+// the node-culling reciprocals (__fdividef, within 2 ulp; a huge finite
+// value for a vanishing component), without the rest of a ray set-up.
+// Conservative: false only when no emitter can be hit.
+__device__ __forceinline__ bool emit_may_hit(const SceneDev& sc, V3 o, V3 d) {
+  if (!sc.has_emit_box) return false;
+  RayPre r;
+  r.ox = o.x;
+  r.oy = o.y;
+  r.oz = o.z;
+  r.ix = fabsf(d.x) > 1e-30f ? __fdividef(1.0f, d.x) : copysignf(1e30f, d.x);
+  r.iy = fabsf(d.y) > 1e-30f ? __fdividef(1.0f, d.y) : copysignf(1e30f, d.y);
+  r.iz = fabsf(d.z) > 1e-30f ? __fdividef(1.0f, d.z) : copysignf(1e30f, d.z);
+  return box_may_hit(r, sc.emit_lo, sc.emit_hi, RAY_TMIN, RAY_TMAX);
 }
 
 // Whether the ray (o, d) may meet the box [lo, hi] inside (tmin, tmax),

@@ -170,16 +170,19 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
     if (sc.lens_radius > 0.0f) {
       // Thin lens (not in the reference, whose camera is a pinhole): the
       // pinhole ray meets the focal plane at distance focal_distance along
-      // the view axis; the origin moves to a uniform point of the lens disk.
+      // the view axis; the origin moves to a uniform point of the lens disk,
+      // drawn by rejection from the square (trig-free, so the oracle draws
+      // the same point bit for bit).
       const V3 wu = v3(sc.unitW[0], sc.unitW[1], sc.unitW[2]);
       const float tf = fdiv(sc.focal_distance, dot(dir, wu));
       const V3 focus = org + tf * dir;
-      const float r = fmul(sc.lens_radius, fsqrt(rnd(seed)));
-      const float phi = fmul(6.28318530717958647692f, rnd(seed));
-      float sp, cp;
-      __sincosf(phi, &sp, &cp);
-      org = org + fmul(r, cp) * v3(sc.unitU[0], sc.unitU[1], sc.unitU[2]) +
-            fmul(r, sp) * v3(sc.unitV[0], sc.unitV[1], sc.unitV[2]);
+      float lu, lv;
+      do {
+        lu = rng11(seed);
+        lv = rng11(seed);
+      } while (fadd(fmul(lu, lu), fmul(lv, lv)) > 1.0f);
+      org = org + fmul(sc.lens_radius, lu) * v3(sc.unitU[0], sc.unitU[1], sc.unitU[2]) +
+            fmul(sc.lens_radius, lv) * v3(sc.unitV[0], sc.unitV[1], sc.unitV[2]);
       dir = normalize(focus - org);
     }
     b.ro[0][slot] = make_float4(org.x, org.y, org.z, __uint_as_float(slot));
@@ -423,7 +426,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
   // the vertex position lives in the shadow ray's origin (s.r.o*)
   V3 N = v3(0.0f), dir = v3(0.0f);
   s.r.ox = s.r.oy = s.r.oz = 0.0f;
-  uint32_t shadow = 0, visits = 0, tests = 0;
+  uint32_t shadow = 0, walked = 0, visits = 0, tests = 0;
   bool pending = false;  // a finished shadow ray not yet evaluated
   __shared__ TriPass tri_pass[4];
   TriPass& tp = tri_pass[threadIdx.x >> 5];
@@ -506,14 +509,35 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
       }
       if (!__any_sync(FULL, have)) break;
       if (have && !ray_active && !pending) {
-        dir = bsdf::shoot_ray_hemisphere(N, seed);
-        ++shadow;
-        ray_active = trav_begin(s, ts, v3(s.r.ox, s.r.oy, s.r.oz), dir, RAY_TMIN, RAY_TMAX);
-        // a ray that cannot reach an emitter only needs to know whether it
-        // hits anything (a miss clears the flag, another hit keeps it), so
-        // its traversal ends at the first hit
-        if (ray_active) s.any = !(sc->has_emit_box && box_may_hit(s.r, sc->emit_lo, sc->emit_hi, RAY_TMIN, RAY_TMAX));
-        pending = !ray_active;  // nothing to traverse: a miss
+        // Draw tries until one needs a traversal.  A ray that cannot reach
+        // an emitter can only miss (the flag is cleared) or hit something
+        // else (the flag is kept): with the flag unset, neither lights the
+        // vertex nor changes the flag, so such a try is counted and its
+        // traversal skipped -- the search's outcome, its flag and the seed
+        // after it are those of tracing every try.  With the flag set, a
+        // ray that cannot reach an emitter is traced to its first hit only
+        // (a hit lights the vertex with the flag's emitter, a miss clears
+        // it); a ray that may reach one is traced to its closest hit.
+        const V3 p = v3(s.r.ox, s.r.oy, s.r.oz);
+        bool capable;
+        while (true) {
+          dir = bsdf::shoot_ray_hemisphere(N, seed);
+          ++shadow;
+          capable = emit_may_hit(*sc, p, dir);
+          if (capable || stale >= 0 || tries + 1 == (uint32_t)NEE_TRIES) break;
+          ++tries;
+        }
+        if (!capable && stale < 0) {
+          s.best_prim = -1;  // the last try, as inconsequential: evaluated as a miss
+          pending = true;
+        } else {
+          ray_active = trav_begin(s, ts, p, dir, RAY_TMIN, RAY_TMAX);
+          if (ray_active) {
+            s.any = !capable;
+            ++walked;
+          }
+          pending = !ray_active;  // nothing to traverse: a miss
+        }
       }
     }
     if (trav_step_warp<COUNT>(ray_active, s, ts, stack, visits, tests, &b.ctrl->status, tp)) {
@@ -522,6 +546,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
     }
   }
   warp_add64(&b.ctrl->rays_shadow, shadow);
+  warp_add64(&b.ctrl->shadow_walked, walked);
   if (COUNT) {
     warp_add64(&b.ctrl->node_visits[1], visits);
     warp_add64(&b.ctrl->tri_tests[1], tests);
@@ -735,6 +760,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
     }
   }
   warp_add64(&b.ctrl->rays_shadow, nshadow);
+  warp_add64(&b.ctrl->shadow_walked, nshadow);  // every shadow ray of this estimator is traced
   if (COUNT) {
     warp_add64(&b.ctrl->node_visits[1], visits);
     warp_add64(&b.ctrl->tri_tests[1], tests);
@@ -832,6 +858,7 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
     }
   });
   warp_add32(&b.ctrl->guided_count, guided_n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.ctrl->infer_rows += *(volatile uint32_t*)&b.ctrl->nee_count;
 }
 
 // ---------------------------------------------------------------------------
@@ -1202,7 +1229,7 @@ Status guide_collect(Renderer& r, int, uint32_t cap, cudaStream_t s) {
 }
 
 // Stage indices of the timer: 0 trace, 1 shade, 2 emitter search, 3 other,
-// 4 guide (inference, sample collection, training, Adam).
+// 4 guide inference, 5 guide training (sample collection, training, Adam).
 Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, lisa_render_stats* st,
                             StageTimer* tm) {
   WaveBufs b = make_bufs(r);
@@ -1217,7 +1244,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       tm->marks.push_back({which, {e0, e1}});
     }
     if (which < 3) launches[which]++;
-    if (which == 4) launches[3]++;
+    if (which == 4 || which == 5) launches[3]++;
     launches[4]++;
     return Status();
   };
@@ -1317,17 +1344,17 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
     }));
     if (guided && waves[wv].train) {
       const uint32_t steps = waves[wv].steps;
-      LISA_TRY(stage(4, [&] { return guide_collect(r, (int)wv, steps * r.guide_chunk, r.stream); }));
+      LISA_TRY(stage(5, [&] { return guide_collect(r, (int)wv, steps * r.guide_chunk, r.stream); }));
       // one Adam step per slice of the collected samples
       for (uint32_t k = 0; k < steps; ++k) {
         GuideSrc slice = train_src;
         slice.first = k * r.guide_chunk;
         slice.n = (k + 1) * r.guide_chunk;
-        LISA_TRY(stage(4, [&] {
+        LISA_TRY(stage(5, [&] {
           return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream,
-                                    true);
+                                    true, &r.ctrl->train_samples);
         }));
-        LISA_TRY(stage(4, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream, slice.count, slice.first); }));
+        LISA_TRY(stage(5, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream, slice.count, slice.first); }));
       }
     }
   }
@@ -1477,7 +1504,13 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
       if (m.first == 0) local.ms_trace += t;
       else if (m.first == 1) local.ms_shade += t;
       else if (m.first == 2) local.ms_nee += t;
-      else if (m.first == 4) local.ms_guide += t;
+      else if (m.first == 4) {
+        local.ms_guide += t;
+        local.ms_guide_infer += t;
+      } else if (m.first == 5) {
+        local.ms_guide += t;
+        local.ms_guide_train += t;
+      }
       else local.ms_other += t;
     }
   }
@@ -1514,6 +1547,9 @@ Status renderer_render(Renderer& r, uint32_t spp_req, bool progressive, lisa_ren
   local.tri_tests_trace = hc.tri_tests[0];
   local.node_visits_nee = hc.node_visits[1];
   local.tri_tests_nee = hc.tri_tests[1];
+  local.shadow_traversals = hc.shadow_walked;
+  local.guide_infer_rows = hc.infer_rows;
+  local.guide_train_samples = hc.train_samples;
   if (st) *st = local;
   if (hc.status) return Status(LISA_ERR_DEVICE, "device status word " + std::to_string(hc.status));
   return Status();

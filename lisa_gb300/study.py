@@ -76,6 +76,8 @@ def hard_indirect(args) -> List[dict]:
                           relmse_corrected=relmse(img, R, vom), guide_loss=st.guide_loss,
                           stages_ms={"trace": st.ms_trace, "shade": st.ms_shade, "nee": st.ms_nee,
                                      "guide": st.ms_guide, "other": st.ms_other},
+                          guide_infer={"ms": st.ms_guide_infer, "rows": st.guide_infer_rows},
+                          guide_train={"ms": st.ms_guide_train, "samples": st.guide_train_samples},
                           launches=st.launches_total)
         r.close()
     tp, tg = rows["plain"]["ms"], rows["guided"]["ms"]

@@ -31,7 +31,8 @@ class OracleScene(C.Structure):
                 ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32), ("bounces", C.c_uint32),
                 ("eye", C.c_float * 3), ("look_at", C.c_float * 3), ("fov", C.c_float),
                 ("rng_mode", C.c_uint32), ("seed", C.c_uint32), ("sample_base", C.c_uint64),
-                ("subframe", C.c_uint32), ("estimator", C.c_uint32)]
+                ("subframe", C.c_uint32), ("estimator", C.c_uint32),
+                ("lens_radius", C.c_float), ("focal_distance", C.c_float)]
 
 
 def build() -> str:
@@ -86,7 +87,8 @@ class Scene:
     """Oracle view of a soup + camera + render settings."""
 
     def __init__(self, vertices, normals, mat_indices, materials, width, height, eye, look_at, fov, spp, bounces,
-                 rng_mode=0, seed=0, sample_base=0, subframe=0, estimator=0):
+                 rng_mode=0, seed=0, sample_base=0, subframe=0, estimator=0, lens_radius=0.0,
+                 focal_distance=0.0):
         self.v = np.ascontiguousarray(np.asarray(vertices, np.float32).reshape(-1, 9))
         self.n = np.ascontiguousarray(np.asarray(normals, np.float32).reshape(-1, 9))
         self.mi = np.ascontiguousarray(np.asarray(mat_indices, np.int32).reshape(-1))
@@ -111,6 +113,7 @@ class Scene:
         s.fov = float(fov)
         s.rng_mode, s.seed, s.sample_base, s.subframe = int(rng_mode), int(seed), int(sample_base), int(subframe)
         s.estimator = int(estimator)  # 0 = the reference estimator, 1 = physically based
+        s.lens_radius, s.focal_distance = float(lens_radius), float(focal_distance)  # thin lens (0 = pinhole)
         self.s = s
 
     @classmethod

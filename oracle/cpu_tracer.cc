@@ -712,6 +712,8 @@ struct oracle_scene {
   uint64_t sample_base;
   uint32_t subframe;
   uint32_t estimator;  // 0 = the reference estimator, 1 = physically based
+  float lens_radius;     // thin lens (the product's option; 0 = pinhole, as the reference)
+  float focal_distance;  // 0 = |W|
 };
 
 static void make_ctx(const oracle_scene* s, int use_bvh, Ctx& c) {
@@ -832,6 +834,15 @@ int oracle_ctx_render(void* ctx, const oracle_scene* s, int threads, uint32_t px
   uvw(s->eye, s->look_at, s->fov, s->width, s->height, U, V, W);
   const V3 eye = v3(s->eye[0], s->eye[1], s->eye[2]);
   const float fw = (float)s->width, fh = (float)s->height;
+  // unit camera axes and focal distance of the thin lens (the same float
+  // steps as the product's scene upload)
+  const float ul = std::sqrt(U.x * U.x + U.y * U.y + U.z * U.z);
+  const float vl = std::sqrt(V.x * V.x + V.y * V.y + V.z * V.z);
+  const float wl = std::sqrt(W.x * W.x + W.y * W.y + W.z * W.z);
+  const V3 uU = ul > 0 ? v3(U.x / ul, U.y / ul, U.z / ul) : v3(0, 0, 0);
+  const V3 uV = vl > 0 ? v3(V.x / vl, V.y / vl, V.z / vl) : v3(0, 0, 0);
+  const V3 uW = wl > 0 ? v3(W.x / wl, W.y / wl, W.z / wl) : v3(0, 0, 0);
+  const float fl_dist = s->focal_distance > 0.0f ? s->focal_distance : wl;
   uint64_t tp = 0, tb = 0, ts = 0;
   if (threads > 0) omp_set_num_threads(threads);
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : tp, tb, ts)
@@ -847,9 +858,23 @@ int oracle_ctx_render(void* ctx, const oracle_scene* s, int threads, uint32_t px
       const float jy = rng11(seed);
       const float dx = (2.0f * (float)x + jx) / fw - 1.0f;
       const float dy = (2.0f * (float)y + jy) / fh - 1.0f;
-      const V3 dir = normalize((dx * U + dy * V) + W);
-      const V3 col = s->estimator == 1 ? trace_path_pb(c, eye, dir, (int)s->bounces, seed, cnt)
-                                       : trace_path(c, eye, dir, (int)s->bounces, seed, cnt);
+      V3 dir = normalize((dx * U + dy * V) + W);
+      V3 org = eye;
+      if (s->lens_radius > 0.0f) {
+        // thin lens: the pinhole ray's point on the focal plane, seen from a
+        // uniform point of the lens disk drawn by rejection from the square
+        const float tf = fl_dist / dot(dir, uW);
+        const V3 focus = org + tf * dir;
+        float lu, lv;
+        do {
+          lu = rng11(seed);
+          lv = rng11(seed);
+        } while (lu * lu + lv * lv > 1.0f);
+        org = org + (s->lens_radius * lu) * uU + (s->lens_radius * lv) * uV;
+        dir = normalize(focus - org);
+      }
+      const V3 col = s->estimator == 1 ? trace_path_pb(c, org, dir, (int)s->bounces, seed, cnt)
+                                       : trace_path(c, org, dir, (int)s->bounces, seed, cnt);
       const float cc[3] = {col.x, col.y, col.z};
       for (int k = 0; k < 3; ++k) {
         a[k] += cc[k];

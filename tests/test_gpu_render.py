@@ -227,3 +227,20 @@ def test_matches_reference_shader_fixture(gpu, tmp_path, name):
     optix = np.fromfile(os.path.join(here, "golden", "optix", name + "_closest.f32"), np.float32).reshape(-1, 3)
     same = (np.abs(optix - img) <= 1e-5 * np.maximum(1.0, np.abs(img))).all(axis=1)
     assert same.mean() >= 0.90, same.mean()
+
+
+@pytest.mark.parametrize("focal", [0.0, 1.2])
+def test_thin_lens_path_by_path(gpu, oracle, focal):
+    """The thin-lens option (aperture > 0; the reference's camera is a
+    pinhole): the lens point is drawn by rejection from the square with the
+    path's own stream, so the oracle traces the same paths.  focal 0 puts
+    the focal plane at |look_at - eye|."""
+    sc = scenes.cornell_box(width=40, height=32, num_samples=4, num_bounces=5)
+    r = L.Renderer(L.params_from_scene(sc), aperture=0.05, focal_distance=focal)
+    st = r.render()
+    img = r.image()
+    ref, _, rays = oracle_mean(oracle, sc, lens_radius=0.05, focal_distance=focal)
+    assert mismatch_fraction(img, ref) <= 0.002
+    assert st.rays_primary == rays[0]
+    pin, _, _ = oracle_mean(oracle, sc)
+    assert mismatch_fraction(img, pin) > 0.3  # the lens changes the image
