@@ -27,12 +27,15 @@ namespace bsdf {
 
 // Uniform point of the cube [-1,1)^3, normalised, flipped into N's
 // hemisphere (src/LiSA/src/maths.cu:10-15).  Draws x, then y, then z.
+__device__ __forceinline__ V3 hemisphere_direction(V3 N, float x, float y, float z) {
+  const V3 r = normalize(v3(x, y, z));
+  return faceforward(r, N, r);
+}
 __device__ __forceinline__ V3 shoot_ray_hemisphere(V3 N, uint32_t& seed) {
   const float x = rng11(seed);
   const float y = rng11(seed);
   const float z = rng11(seed);
-  const V3 r = normalize(v3(x, y, z));
-  return faceforward(r, N, r);
+  return hemisphere_direction(N, x, y, z);
 }
 
 // Schlick (src/LiSA/src/maths.cu:17-20)

@@ -79,4 +79,18 @@ __device__ __forceinline__ float rnd(uint32_t& s) { return fmul((float)lcg(s), 5
 // [-1, 1): rnd*2 - 1
 __device__ __forceinline__ float rng11(uint32_t& s) { return fsub(fmul(rnd(s), 2.0f), 1.0f); }
 
+// k LCG steps at once: the state after them is a * state + c (mod 2^32),
+// with a = A^k and c = C (A^(k-1) + ... + A + 1) for the step's A and C.
+struct LcgJump {
+  uint32_t a, c;
+};
+__device__ __forceinline__ LcgJump lcg_jump(uint32_t k) {
+  LcgJump j{1u, 0u};
+  for (uint32_t i = 0; i < k; ++i) {
+    j.a *= 1664525u;
+    j.c = j.c * 1664525u + 1013904223u;
+  }
+  return j;
+}
+
 }  // namespace lisa

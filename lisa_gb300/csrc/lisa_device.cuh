@@ -562,6 +562,30 @@ __device__ __forceinline__ bool emit_may_hit(const SceneDev& sc, V3 o, V3 d) {
   return box_may_hit(r, sc.emit_lo, sc.emit_hi, RAY_TMIN, RAY_TMAX);
 }
 
+// Conservative emit_may_hit for a hemisphere draw (x, y, z) of
+// shoot_ray_hemisphere before it is normalised and flipped.  The draw,
+// flipped by the sign of dot(N, draw), points along the same ray as the
+// exact direction (a positive multiple, up to the direction's own
+// rounding, which the slab padding covers); testing it on (0, inf) covers
+// every point of (RAY_TMIN, RAY_TMAX) along the exact direction.  Where
+// dot(N, draw) is too near zero for its sign to be certain (a few ulp of
+// the exact dot would be), or not a number, the answer is "may hit".
+__device__ __forceinline__ bool emit_may_hit_draw(const SceneDev& sc, V3 o, V3 N, float x, float y, float z) {
+  if (!sc.has_emit_box) return false;
+  const float s = N.x * x + N.y * y + N.z * z;
+  if (!(fabsf(s) > 1e-5f * (fabsf(x) + fabsf(y) + fabsf(z)))) return true;
+  const float f = s > 0.0f ? 1.0f : -1.0f;
+  const float dx = f * x, dy = f * y, dz = f * z;
+  RayPre r;
+  r.ox = o.x;
+  r.oy = o.y;
+  r.oz = o.z;
+  r.ix = fabsf(dx) > 1e-30f ? __fdividef(1.0f, dx) : copysignf(1e30f, dx);
+  r.iy = fabsf(dy) > 1e-30f ? __fdividef(1.0f, dy) : copysignf(1e30f, dy);
+  r.iz = fabsf(dz) > 1e-30f ? __fdividef(1.0f, dz) : copysignf(1e30f, dz);
+  return box_may_hit(r, sc.emit_lo, sc.emit_hi, 0.0f, 3.0e38f);
+}
+
 // Whether the ray (o, d) may meet the box [lo, hi] inside (tmin, tmax),
 // every step a single IEEE rounding so the host oracle takes the same
 // decision bit for bit: slab distances with the correctly rounded 1/d (a

@@ -428,6 +428,14 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
   s.r.ox = s.r.oy = s.r.oz = 0.0f;
   uint32_t shadow = 0, walked = 0, visits = 0, tests = 0;
   bool pending = false;  // a finished shadow ray not yet evaluated
+  // LCG jumps over j tries (3 draws each), j = 0..31, for the warp's
+  // search of the next try that needs a traversal
+  __shared__ uint2 s_jump[32];
+  if (threadIdx.x < 32) {
+    const LcgJump j = lcg_jump(3u * threadIdx.x);
+    s_jump[threadIdx.x] = make_uint2(j.a, j.c);
+  }
+  __syncthreads();
   __shared__ TriPass tri_pass[4];
   TriPass& tp = tri_pass[threadIdx.x >> 5];
   while (true) {
@@ -508,27 +516,63 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
         }
       }
       if (!__any_sync(FULL, have)) break;
-      if (have && !ray_active && !pending) {
-        // Draw tries until one needs a traversal.  A ray that cannot reach
-        // an emitter can only miss (the flag is cleared) or hit something
-        // else (the flag is kept): with the flag unset, neither lights the
-        // vertex nor changes the flag, so such a try is counted and its
-        // traversal skipped -- the search's outcome, its flag and the seed
-        // after it are those of tracing every try.  With the flag set, a
-        // ray that cannot reach an emitter is traced to its first hit only
-        // (a hit lights the vertex with the flag's emitter, a miss clears
-        // it); a ray that may reach one is traced to its closest hit.
-        const V3 p = v3(s.r.ox, s.r.oy, s.r.oz);
-        bool capable;
-        while (true) {
-          dir = bsdf::shoot_ray_hemisphere(N, seed);
-          ++shadow;
-          capable = emit_may_hit(*sc, p, dir);
-          if (capable || stale >= 0 || tries + 1 == (uint32_t)NEE_TRIES) break;
-          ++tries;
+      // The next try of a vertex.  A ray that cannot reach an emitter can
+      // only miss (the flag is cleared) or hit something else (the flag is
+      // kept): with the flag unset, neither lights the vertex nor changes
+      // the flag, so such a try is counted and its traversal skipped -- the
+      // search's outcome, the flag it leaves and the seed after it are those
+      // of tracing every try.  With the flag set, a ray that cannot reach an
+      // emitter is traced to its first hit only (a hit lights the vertex
+      // with the flag's emitter, a miss clears it); a ray that may reach one
+      // is traced to its closest hit.
+      //
+      // For the vertices whose flag is unset, the warp finds the next try
+      // that may reach an emitter together: the LCG jumps to the state
+      // before each later try, so lane j tests try `tries + j` of one
+      // vertex (a conservative test on the unnormalised draw), and the first
+      // lane that may (or the vertex's last try) sets where the vertex goes
+      // on.  The tries before it are passed over without their directions.
+      const bool search = have && !ray_active && !pending && stale < 0;
+      uint32_t smask = __ballot_sync(FULL, search);
+      uint32_t skipped = 0;
+      while (smask) {
+        const int owner = __ffs(smask) - 1;
+        smask &= smask - 1;
+        const uint32_t s0 = __shfl_sync(FULL, seed, owner);
+        const uint32_t t0 = __shfl_sync(FULL, tries, owner);
+        const V3 po = v3(__shfl_sync(FULL, s.r.ox, owner), __shfl_sync(FULL, s.r.oy, owner),
+                         __shfl_sync(FULL, s.r.oz, owner));
+        const V3 no = v3(__shfl_sync(FULL, N.x, owner), __shfl_sync(FULL, N.y, owner), __shfl_sync(FULL, N.z, owner));
+        const SceneDev* so = (const SceneDev*)__shfl_sync(FULL, (unsigned long long)sc, owner);
+        const uint32_t t = t0 + (uint32_t)lane;
+        bool cand = t + 1 == (uint32_t)NEE_TRIES;
+        if (t + 1 < (uint32_t)NEE_TRIES) {
+          const uint2 j = s_jump[lane];
+          uint32_t st = j.x * s0 + j.y;
+          const float hx = rng11(st);
+          const float hy = rng11(st);
+          const float hz = rng11(st);
+          cand = emit_may_hit_draw(*so, po, no, hx, hy, hz);
         }
+        // the vertex's last try is always a candidate, so a lane is found
+        const int first = __ffs(__ballot_sync(FULL, cand)) - 1;
+        if (lane == owner) {
+          const uint2 j = s_jump[first];
+          seed = j.x * seed + j.y;
+          tries = t0 + (uint32_t)first;
+          skipped = (uint32_t)first;
+        }
+      }
+      if (have && !ray_active && !pending) {
+        const V3 p = v3(s.r.ox, s.r.oy, s.r.oz);
+        shadow += skipped + 1;
+        const float hx = rng11(seed);
+        const float hy = rng11(seed);
+        const float hz = rng11(seed);
+        dir = bsdf::hemisphere_direction(N, hx, hy, hz);
+        const bool capable = emit_may_hit(*sc, p, dir);
         if (!capable && stale < 0) {
-          s.best_prim = -1;  // the last try, as inconsequential: evaluated as a miss
+          s.best_prim = -1;  // an inconsequential try: evaluated as a miss
           pending = true;
         } else {
           ray_active = trav_begin(s, ts, p, dir, RAY_TMIN, RAY_TMAX);

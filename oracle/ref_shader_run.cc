@@ -111,6 +111,7 @@ struct OracleScene {
   uint32_t rng_mode, seed;
   uint64_t sample_base;
   uint32_t subframe, estimator;
+  float lens_radius, focal_distance;
 };
 
 struct Frame {
