@@ -554,7 +554,7 @@ struct CollapseArgs {
   const int32_t* mats;  // material per triangle, or null
   uint4* nodes;
   float4* tris;
-  uint32_t* counters;  // [0] nodes, [1] tri slots, [2] next work count
+  uint32_t* counters;  // [0] nodes, [1] tri slots
 };
 
 __device__ __forceinline__ uint32_t sub_count(const CollapseArgs& a, uint32_t c) {
@@ -575,10 +575,30 @@ __device__ int grid_exponent(double ext) {
   return max(-126, min(127, e));
 }
 
-__global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ work, uint32_t nwork, uint2* __restrict__ next) {
-  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nwork) return;
-  const uint32_t dst = work[w].x, src = work[w].y;
+// Collapse levels run as a fixed sequence of launches with no host round
+// trip: level l reads its work count from levels[l] (written by level l-1)
+// and appends the next level's work, counting it in levels[l+1]; a level
+// with no work returns at once.
+constexpr int COLLAPSE_LAUNCHES = 24;
+
+__global__ void k_collapse_init(uint32_t* counters, uint32_t* levels, uint2* work0, uint2 root) {
+  counters[0] = 1u;  // node 0 is the root
+  counters[1] = 0u;
+  for (int l = 0; l <= COLLAPSE_LAUNCHES + 1; ++l) levels[l] = l == 0 ? 1u : 0u;
+  work0[0] = root;
+}
+
+__device__ void collapse_one(const CollapseArgs& a, uint2 item, uint2* __restrict__ next, uint32_t* next_count);
+
+__global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ work, const uint32_t* __restrict__ nwork_p,
+                           uint2* __restrict__ next, uint32_t* next_count) {
+  const uint32_t nwork = *nwork_p;
+  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwork; w += gridDim.x * blockDim.x)
+    collapse_one(a, work[w], next, next_count);
+}
+
+__device__ void collapse_one(const CollapseArgs& a, uint2 item, uint2* __restrict__ next, uint32_t* next_count) {
+  const uint32_t dst = item.x, src = item.y;
   uint32_t cand[8];
   int nc;
   if (!(src & LEAF_BIT) && sub_count(a, src) > 3u) {
@@ -658,7 +678,7 @@ __global__ void k_collapse(CollapseArgs a, const uint2* __restrict__ work, uint3
     if (cnt > 3u) {
       imask |= 1u << k;
       meta[k] = (uint8_t)rank;
-      const uint32_t slot = atomicAdd(&a.counters[2], 1u);
+      const uint32_t slot = atomicAdd(next_count, 1u);
       next[slot] = make_uint2(child_base + rank, cand[k]);
       ++rank;
     } else {
@@ -752,6 +772,7 @@ size_t bvh_temp_bytes(uint32_t n) {
   b += al256(4ull * 256 * tiles) + al256(4ull * (cdiv(256ull * tiles, SCAN_CHUNK) + 16));
   b += 7 * al256(4ull * n);                                    // tree links and flags
   b += al256(16) + al256(48);                                  // counters, bounds
+  b += al256(4ull * 32);                                       // collapse level counts
   b += 2 * al256(8ull * (n + 1));                              // collapse work lists
   return (size_t)b;
 }
@@ -795,6 +816,8 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource
   LISA_TRY(take(tmp, &par_leaf, n, w));
   LISA_TRY(take(tmp, &flags, n, w));
   LISA_TRY(take(tmp, &counters, 4, w));
+  uint32_t* levels = nullptr;
+  LISA_TRY(take(tmp, &levels, 32, w));
   LISA_TRY(take(tmp, &bounds, 12, w));
   LISA_TRY(take(tmp, &work0, n + 1, w));
   LISA_TRY(take(tmp, &work1, n + 1, w));
@@ -826,25 +849,46 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource
   float4* tris = nullptr;
   LISA_TRY(take(out, &nodes, 5ull * (n + 1), "bvh nodes"));
   LISA_TRY(take(out, &tris, 3ull * n, "bvh triangles"));
-  uint32_t hc[4] = {1u, 0u, 0u, 0u};  // node 0 is the root
-  LISA_CUDA(cudaMemcpyAsync(counters, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
   const uint2 root = make_uint2(0u, n > 1 ? 0u : LEAF_BIT);
-  LISA_CUDA(cudaMemcpyAsync(work0, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+  k_collapse_init<<<1, 1, 0, s>>>(counters, levels, work0, root);
+  LISA_CUDA(cudaGetLastError());
   CollapseArgs a{n, vals, plo, phi, ilo, ihi, left, right, first, d_verts, d_mat, nodes, tris, counters};
-  uint32_t nwork = 1, depth = 0;
-  uint2 *wi = work0, *wo = work1;
-  while (nwork > 0) {
-    LISA_CUDA(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), s));
-    k_collapse<<<cdiv(nwork, 64), 64, 0, s>>>(a, wi, nwork, wo);
-    LISA_CUDA(cudaGetLastError());
-    LISA_CUDA(cudaMemcpyAsync(&nwork, counters + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    LISA_CUDA(cudaStreamSynchronize(s));
-    std::swap(wi, wo);
-    ++depth;
-  }
+  // a level holds at most one work item per 8-wide node, fewer than n/2
+  int dev = 0, sms = 0;
+  LISA_CUDA(cudaGetDevice(&dev));
+  LISA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t cgrid = std::max<uint32_t>(1u, std::min<uint32_t>(cdiv(n / 2 + 1, 64), (uint32_t)sms * 16u));
+  for (int l = 0; l < COLLAPSE_LAUNCHES; ++l)
+    k_collapse<<<cgrid, 64, 0, s>>>(a, (l & 1) ? work1 : work0, levels + l, (l & 1) ? work0 : work1,
+                                    levels + l + 1);
+  LISA_CUDA(cudaGetLastError());
+  uint32_t hc[2];
+  uint32_t hl[COLLAPSE_LAUNCHES + 1];
   LISA_CUDA(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  LISA_CUDA(cudaMemcpyAsync(hl, levels, sizeof(hl), cudaMemcpyDeviceToHost, s));
   LISA_CUDA(cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s));
   LISA_CUDA(cudaStreamSynchronize(s));
+  uint32_t depth = 0;
+  while (depth < (uint32_t)COLLAPSE_LAUNCHES && hl[depth] > 0) ++depth;
+  if (depth == (uint32_t)COLLAPSE_LAUNCHES && hl[COLLAPSE_LAUNCHES] > 0) {
+    // a tree deeper than the fixed launches: the remaining levels, one host
+    // round trip each (slot C holds the level's count, slot C+1 the next's)
+    uint32_t* cur = levels + COLLAPSE_LAUNCHES;
+    uint32_t nwork = hl[COLLAPSE_LAUNCHES];
+    uint2 *wi = (COLLAPSE_LAUNCHES & 1) ? work1 : work0, *wo = (COLLAPSE_LAUNCHES & 1) ? work0 : work1;
+    while (nwork > 0) {
+      LISA_CUDA(cudaMemsetAsync(cur + 1, 0, sizeof(uint32_t), s));
+      k_collapse<<<cdiv(nwork, 64), 64, 0, s>>>(a, wi, cur, wo, cur + 1);
+      LISA_CUDA(cudaGetLastError());
+      LISA_CUDA(cudaMemcpyAsync(cur, cur + 1, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+      LISA_CUDA(cudaMemcpyAsync(&nwork, cur + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      LISA_CUDA(cudaStreamSynchronize(s));
+      std::swap(wi, wo);
+      ++depth;
+    }
+    LISA_CUDA(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    LISA_CUDA(cudaStreamSynchronize(s));
+  }
   if (hc[1] != n) return Status(LISA_ERR_DEVICE, "bvh build: leaf triangle count mismatch");
   info->num_nodes = hc[0];
   info->num_tri_slots = hc[1];

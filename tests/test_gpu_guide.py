@@ -2,9 +2,13 @@
 
 Forward outputs, training-loss gradients (FP32 gradients from BF16
 tensor-core products) and the Adam update are compared with
-oracle/guide_ref.py, which rounds to BF16 at the same points.  Tolerances:
-outputs within 2e-2 relative to their scale; per-block gradient cosine
-similarity >= 0.999 and relative L2 error <= 3e-2.
+oracle/guide_ref.py, which rounds to BF16 at the same points, so only the
+FP32 accumulation order differs (and, rarely, a BF16 rounding of an
+activation that this order tips).  Tolerances, about three times the
+errors measured on a GB300 (forward 5.9e-4 of the output scale, gradient
+blocks 3.2e-4 relative at worst): outputs within 2e-3 of their scale;
+per-block gradient cosine similarity >= 1 - 1e-6 and relative L2 error
+<= 1e-3.
 """
 import numpy as np
 import pytest
@@ -43,7 +47,7 @@ def test_forward_matches_oracle(gpu):
     ref, _ = G.forward(p, X, bf=True)
     scale = np.abs(ref).max()
     err = np.abs(out - ref).max() / scale
-    assert err < 2e-2, err
+    assert err < 2e-3, err
     assert np.corrcoef(out.ravel(), ref.ravel())[0, 1] > 0.9999
 
 
@@ -59,7 +63,7 @@ def test_training_gradients_match_oracle(gpu):
         x, y = grads[a:b].astype(np.float64), rg[a:b]
         cos = x @ y / (np.linalg.norm(x) * np.linalg.norm(y) + 1e-30)
         rel = np.linalg.norm(x - y) / (np.linalg.norm(y) + 1e-30)
-        assert cos >= 0.999 and rel <= 3e-2, (name, cos, rel)
+        assert cos >= 1.0 - 1e-6 and rel <= 1e-3, (name, cos, rel)
 
 
 def test_adam_update(gpu):

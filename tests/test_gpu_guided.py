@@ -80,6 +80,30 @@ def test_hard_indirect_guided_vs_plain(gpu, capsys):
     assert e_g <= 1.15 * e_p
 
 
+def test_guide_halves_time_to_plain_error(gpu, capsys):
+    """What the trained guide gains, at equal time.  The hard-indirect scene
+    (the 1.31M-triangle displaced icosphere in the box, its light shrunk to
+    0.02 x 0.02 behind a baffle), 1024 x 1024, 256 spp, 8 bounces,
+    physically based estimator: plain and guided renders against a
+    4,096-spp plain reference accumulated in FP64, relMSE with the
+    reference's own variance removed, device times measured by the
+    renderer.  The guided render must reach the plain render's error in at
+    most 0.6 of the plain render's time (measured: about 0.27)."""
+    import argparse
+
+    from lisa_gb300 import study
+
+    a = argparse.Namespace(res=1024, level=8, spp=256, ref_spp=4096, ref_chunk=256, estimator="physical")
+    q = study.hard_indirect(a)[0]
+    ratio = q["time_to_plain_error"]
+    with capsys.disabled():
+        print(f"\nhard indirect 1024x1024 @256 spp (physically based): plain {q['plain']['ms']:.1f} ms relMSE "
+              f"{q['plain']['relmse_corrected']:.3e}, guided {q['guided']['ms']:.1f} ms relMSE "
+              f"{q['guided']['relmse_corrected']:.3e}, time to plain's error {ratio:.3f}x")
+    assert q["guided"]["guide_train"]["samples"] > 0 and q["guided"]["guide_infer"]["rows"] > 0
+    assert ratio is not None and ratio <= 0.6, ratio
+
+
 def test_low_spp_scenes_render_plain_in_a_guided_batch(gpu):
     """Guided mode guides the scenes with at least guide_min_spp samples; a
     scene below it renders on the plain path (same image as a plain
