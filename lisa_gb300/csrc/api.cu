@@ -242,6 +242,63 @@ __global__ void k_emit_of_prim(int32_t* m, uint32_t n, const int32_t* em, uint32
   }
 }
 
+// Leaf triangles of the emitters' own BVH carry their index among the
+// emitters; make it the scene-wide triangle index (the tie rule compares
+// scene-wide indices).
+__global__ void k_emit_global_ids(float4* tris, uint32_t n, const int32_t* __restrict__ global) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int local = __float_as_int(tris[3ull * k].w);
+    tris[3ull * k].w = __int_as_float(global[local]);
+  }
+}
+
+// BVH over the scene's emissive triangles, built like the scene's (same
+// builder, so the same exact traversal); leaves carry scene-wide triangle
+// indices and emitter materials.
+Status build_emitter_bvh(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
+  std::vector<float> ev;
+  std::vector<int32_t> gid, emat;
+  const uint32_t T = (uint32_t)(p.num_vertices / 3);
+  for (uint32_t t = 0; t < T; ++t) {
+    const int32_t m = p.mat_indices[t];
+    if (m < 0 || m >= p.num_materials || !p.materials[m].emit) continue;
+    for (int j = 0; j < 3; ++j) {
+      const lisa_float3& v = p.vertices[3ull * t + j];
+      ev.push_back(v.x);
+      ev.push_back(v.y);
+      ev.push_back(v.z);
+    }
+    gid.push_back((int32_t)t);
+    emat.push_back(m);
+  }
+  const uint32_t ne = (uint32_t)gid.size();
+  if (!ne) return Status();
+  float* d_ev = nullptr;
+  int32_t *d_gid = nullptr, *d_emat = nullptr;
+  cudaError_t e = cudaMalloc(&d_ev, sizeof(float) * ev.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d_gid, sizeof(int32_t) * ne);
+  if (e == cudaSuccess) e = cudaMalloc(&d_emat, sizeof(int32_t) * ne);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_ev, ev.data(), sizeof(float) * ev.size(), cudaMemcpyHostToDevice, r.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_gid, gid.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, r.stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_emat, emat.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, r.stream);
+  Status st = e == cudaSuccess ? Status() : Status::cuda(e, "emitter BVH upload");
+  if (st.ok()) {
+    TempDeviceBufs tmp;
+    st = build_bvh(d_ev, ne, r.stream, tmp, r.arena, &s.enodes, &s.etris, &s.ebvh, d_emat, r.opts.bvh_lbvh_only == 0);
+    if (st.ok()) {
+      k_emit_global_ids<<<r.sm_count * 4, 256, 0, r.stream>>>(s.etris, ne, d_gid);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);
+      if (e != cudaSuccess) st = Status::cuda(e, "emitter BVH indices");
+    }
+  }
+  if (d_ev) cudaFree(d_ev);
+  if (d_gid) cudaFree(d_gid);
+  if (d_emat) cudaFree(d_emat);
+  return st;
+}
+
 Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   LISA_TRY(validate(p));
   s.params = p;
@@ -327,6 +384,8 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
       s.emit_hi[k] = any ? hi[k] + pad : 0.0f;
     }
   }
+  // the emitters' own BVH (reference estimator's emitter search)
+  if (r.opts.estimator != LISA_ESTIMATOR_PHYSICAL && s.has_emit_box) LISA_TRY(build_emitter_bvh(r, p, s));
   // materials
   std::vector<DevMaterial> dm(std::max(p.num_materials, 1));
   for (int i = 0; i < p.num_materials; ++i) dm[i] = to_dev(p.materials[i]);
@@ -357,6 +416,10 @@ SceneDev scene_dev(const Renderer& r, const SceneGpu& s) {
   d.mats = s.mats;
   d.num_prims = s.num_prims;
   d.num_nodes = s.bvh.num_nodes;
+  d.enodes = s.enodes;
+  d.etris = s.etris;
+  d.num_enodes = s.enodes ? s.ebvh.num_nodes : 0u;
+  d.num_etris = s.enodes ? s.ebvh.num_tri_slots : 0u;
   d.num_mats = (uint32_t)std::max(s.params.num_materials, 0);
   d.extent = s.extent;
   d.width = s.params.width;

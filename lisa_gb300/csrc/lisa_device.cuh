@@ -94,6 +94,12 @@ struct SceneDev {
   uint32_t num_emit;
   uint32_t has_emit_box;     // the scene has emissive triangles, all inside emit_lo..emit_hi
   float emit_lo[3], emit_hi[3];
+  // BVH over the emissive triangles alone (0 nodes = none): the emitter
+  // search asks it first whether a ray meets an emitter at all
+  const uint4* enodes;
+  const float4* etris;
+  uint32_t num_enodes;
+  uint32_t num_etris;
 };
 
 // One group of a wave: `nplanes` consecutive sample planes of pixels
@@ -265,6 +271,20 @@ __device__ __forceinline__ TraceScene trace_scene(const SceneDev& sc) {
   return t;
 }
 
+// The emissive triangles' own BVH, with the scene's extent (the ray set-up
+// and so every triangle test are those of the scene's BVH).
+__device__ __forceinline__ TraceScene trace_scene_emit(const SceneDev& sc) {
+  TraceScene t;
+  t.nodes = sc.enodes;
+  t.tris = sc.etris;
+  t.num_nodes = sc.num_enodes;
+  t.extent = sc.extent;
+#ifdef LISA_BOUNDS
+  t.num_tris = sc.num_etris;
+#endif
+  return t;
+}
+
 constexpr uint32_t NODE_NONE = 0xffffffffu;
 
 struct TravState {
@@ -278,7 +298,7 @@ struct TravState {
   int best_mat;  // emitter material of the best hit, -1 if not an emitter (from the leaf triangle)
   uint32_t node;
   int sp;
-  bool any;  // stop at the first hit found (only whether there is one matters)
+  bool any;  // stop at the first non-emitter hit found (see trav_pop)
 };
 
 __device__ __forceinline__ float byte_f(uint32_t w, int b) { return (float)((w >> (8 * b)) & 0xffu); }
@@ -612,7 +632,11 @@ __device__ __forceinline__ bool box_may_hit_exact(V3 o, V3 d, const float* lo, c
 // and moves to the nearest child not culled.  Returns true when the
 // traversal is finished.
 __device__ __forceinline__ bool trav_pop(TravState& s, uint2* stack, int sp0) {
-  if (s.any && s.best_prim >= 0) return true;
+  // an any-hit traversal ends at its first hit that is not an emitter's (a
+  // ray that cannot reach an emitter only finds such hits; the emitter
+  // search's scene pass starts from an emitter hit and looks for a nearer
+  // triangle, which cannot be an emitter's)
+  if (s.any && s.best_prim >= 0 && s.best_mat < 0) return true;
   // (entry distances are positive, so their bit patterns order as floats)
   const int sp = s.sp;
   for (int i = sp0 + 1; i < sp; ++i) {

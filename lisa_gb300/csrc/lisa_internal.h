@@ -136,6 +136,11 @@ struct SceneGpu {
   // device
   uint4* nodes = nullptr;
   float4* tris = nullptr;
+  // BVH over the emissive triangles alone (reference estimator): leaves
+  // carry the triangles' scene-wide indices and their emitter materials
+  BvhBuildResult ebvh{};
+  uint4* enodes = nullptr;
+  float4* etris = nullptr;
   float4* prims = nullptr;
   DevMaterial* mats = nullptr;
   float4* acc_sum = nullptr;

@@ -36,9 +36,11 @@
 namespace lisa {
 
 constexpr uint32_t FULL = 0xffffffffu;
+// emissive triangles from which the emitter search uses their own BVH
+constexpr uint32_t EMIT_BVH_MIN_TRIS = 32;
 
 #ifndef LISA_NEE_MIN_BLOCKS
-#define LISA_NEE_MIN_BLOCKS 7  // 7 x 128 threads per SM (72 registers; measured best of 6..10)
+#define LISA_NEE_MIN_BLOCKS 6  // 6 x 128 threads per SM (80 registers; measured best of 6..8)
 #endif
 #ifndef LISA_NEE_PB_MIN_BLOCKS
 #define LISA_NEE_PB_MIN_BLOCKS 7  // physically based emitter kernel: 7 x 128 threads per SM
@@ -428,6 +430,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
   s.r.ox = s.r.oy = s.r.oz = 0.0f;
   uint32_t shadow = 0, walked = 0, visits = 0, tests = 0;
   bool pending = false;  // a finished shadow ray not yet evaluated
+  bool emit_pass = false;  // the finished traversal was of the emitters' own BVH
   // LCG jumps over j tries (3 draws each), j = 0..31, for the warp's
   // search of the next try that needs a traversal
   __shared__ uint2 s_jump[32];
@@ -446,6 +449,29 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
     if (__popc(busy) <= (int)b.refill_busy_max) {
       bool want_ray = false;
       V3 nd = v3(0.0f);
+      if (pending && emit_pass) {
+        // A try with the flag unset matters only if its closest hit is an
+        // emitter.  The emitters' BVH gave the nearest emitter on the ray
+        // (if none, the try is inconsequential: evaluated as a miss); the
+        // scene's BVH, started from that hit as the best so far, keeps it
+        // unless a triangle is nearer (or as near with a lower index) --
+        // the same closest hit as one traversal of the whole scene.  Such a
+        // triangle is not an emitter's, so that pass ends at the first one.
+        emit_pass = false;
+        if (s.best_prim >= 0) {
+          const float te = s.best_t;
+          const int pe = s.best_prim, me = s.best_mat;
+          ts = trace_scene(*sc);
+          ray_active = trav_begin(s, ts, v3(s.r.ox, s.r.oy, s.r.oz), dir, RAY_TMIN, RAY_TMAX);
+          s.best_t = te;
+          s.best_prim = pe;
+          s.best_mat = me;
+          s.cull = fmaf(te, 1.52587890625e-5f, te) + s.r.slack;
+          s.any = true;
+          ++walked;
+          pending = !ray_active;
+        }
+      }
       if (pending) {
         pending = false;
         if (s.best_prim >= 0) {
@@ -575,10 +601,17 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
           s.best_prim = -1;  // an inconsequential try: evaluated as a miss
           pending = true;
         } else {
+          // with the flag unset, a ray that may reach an emitter first asks
+          // the emitters' own BVH (scenes with more than a few emitter
+          // triangles; with a few, the bounds test above is as selective)
+          emit_pass = stale < 0 && sc->num_etris >= EMIT_BVH_MIN_TRIS;
+          ts = emit_pass ? trace_scene_emit(*sc) : trace_scene(*sc);
           ray_active = trav_begin(s, ts, p, dir, RAY_TMIN, RAY_TMAX);
           if (ray_active) {
             s.any = !capable;
             ++walked;
+          } else {
+            emit_pass = false;
           }
           pending = !ray_active;  // nothing to traverse: a miss
         }
