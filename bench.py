@@ -44,7 +44,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = ("displaced icosphere 1,310,720 tris (dielectric n=1.5) in Cornell box, 1024x1024, 8 bounces, "
             "16 spp per step (256-spp frame = 16 steps), compat estimator")
-METRIC = "Mrays/s (primary+bounce+shadow rays traced)"
+METRIC = "Mrays/s (primary+bounce+shadow rays of the reference estimator, counted as its shader.cu traces them)"
 
 
 def dist_init(gpus: int):
@@ -185,20 +185,27 @@ def measured_peak_hbm():
         return 6800.0, "of fallback"
 
 
+TRAFFIC_FILE = os.path.join("profiles", "dram_traffic_icosphere1310k_1024px.md")
+
+
 def profile_traffic():
-    """Per-launch DRAM bytes of the emitter-search kernel from the committed
-    ncu summary (profiles/nee_traffic.txt, key=value lines), or None."""
-    p = os.path.join(ROOT, "profiles", "nee_traffic.txt")
+    """DRAM bytes per unit of the path's kernels, measured by ncu on this
+    workload (the committed summary's key = value lines), or {}."""
     try:
         kv = {}
-        with open(p) as f:
+        with open(os.path.join(ROOT, TRAFFIC_FILE)) as f:
             for ln in f:
-                if "=" in ln and not ln.startswith("#"):
-                    k, v = ln.split("=", 1)
-                    kv[k.strip()] = v.strip()
-        return float(kv["dram_bytes_per_vertex"])
-    except (OSError, KeyError, ValueError):
-        return None
+                k, sep, v = ln.partition(" = ")
+                if not sep or " " in k.strip() or not k.strip().startswith("k_"):
+                    continue
+                v = v.strip()
+                try:
+                    kv[k.strip()] = float(v)
+                except ValueError:
+                    kv[k.strip()] = v
+        return kv
+    except OSError:
+        return {}
 
 
 def make_scene(level=8, res=1024):
@@ -207,14 +214,39 @@ def make_scene(level=8, res=1024):
     return scenes.icosphere_box(level=level, width=res, height=res, num_samples=256, num_bounces=8)
 
 
-# algorithmic bytes of the emitter-search kernel (k_nee): per opaque vertex
-# the queue entry (48 B) + path state read and written back (36 + 36 B) + the
-# continuation ray (32 B); per shadow ray the material look-up of the hit
-# (16 B); per node visit 80 B; per triangle test 48 B.
+# Algorithmic bytes.  Closest-hit kernel (k_trace), per radiance ray: the
+# queued ray read (32 B) and its hit written (8 B); per node visit 80 B; per
+# triangle test 48 B.  Emitter-search kernel (k_nee), per opaque vertex: the
+# queue entry (48 B) + path state read and written back (36 + 36 B) + the
+# continuation ray (32 B); per shadow ray that walks a BVH the material
+# look-up of its hit (16 B); node visits and triangle tests as above.  (A try
+# that cannot change the search's result moves no bytes.)
+TRACE_B_RAY = 32 + 8
 NEE_B_VERTEX = 48 + 36 + 36 + 32
 NEE_B_RAY = 16
 B_NODE = 80
 B_TRI = 48
+
+
+def kernel_roofline(name, ms_total, launches, bytes_step, launches_counted, peak, peak_kind, dram_per_unit,
+                    units_step, limiter, extra):
+    """HBM roofline of one kernel: algorithmic bytes per launch (the counting
+    pass's per-step counts x the per-unit bytes, over its launches) over the
+    kernel's average CUDA-event launch time; traffic = ncu's DRAM bytes per
+    unit on this workload x the units of a launch (a measured rate scaled to
+    the launch, not a capture of this run)."""
+    bytes_launch = bytes_step / max(launches_counted, 1)
+    avg_s = ms_total / 1e3 / max(launches, 1)
+    achieved = bytes_launch / avg_s / 1e9 if avg_s > 0 else 0.0
+    traffic = None if dram_per_unit is None else dram_per_unit * units_step / max(launches_counted, 1)
+    out = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+           "traffic_kind": "ncu DRAM bytes per unit on this workload, scaled to a launch",
+           "dram_gbs_from_traffic": (traffic / avg_s / 1e9) if (traffic and avg_s > 0) else None,
+           "limiter": limiter, "bytes_per_launch": bytes_launch, "avg_launch_ms": avg_s * 1e3,
+           "ms_in_timed_region": ms_total}
+    out.update(extra)
+    return out
 
 
 def cpu_sample(scene, spp, budget_s=12.0, threads=0, seed=0):
@@ -447,14 +479,30 @@ def run_ours(args, rank, ws, local):
     rc = L.Renderer(params, copts)
     rc.set_sample_offset(shard_first)
     cs = rc.render_progressive(args.spp_per_step)
-    nee_bytes_step = (cs.nee_vertices * NEE_B_VERTEX + cs.rays_shadow * NEE_B_RAY +
-                      cs.node_visits_nee * B_NODE + cs.tri_tests_nee * B_TRI)
-    nee_bytes_launch = nee_bytes_step / max(cs.launches_nee, 1)
-    avg_nee_s = nee_ms / 1e3 / max(nee_launches, 1)
-    achieved = nee_bytes_launch / avg_nee_s / 1e9
     peak, peak_kind = measured_peak_hbm()
-    tpv = profile_traffic()
-    traffic = None if tpv is None else tpv * cs.nee_vertices / max(cs.launches_nee, 1)
+    dram = profile_traffic()
+    radiance = cs.rays_primary + cs.rays_bounce
+    kernels = {
+        "k_trace": kernel_roofline(
+            "k_trace (closest hit of radiance rays)", trace_ms, sum(s.launches_trace for s in stats),
+            radiance * TRACE_B_RAY + cs.node_visits_trace * B_NODE + cs.tri_tests_trace * B_TRI,
+            cs.launches_trace, peak, peak_kind, dram.get("k_trace_dram_bytes_per_ray"), radiance,
+            dram.get("k_trace_limiter"),
+            {"per_unit": {"ray_B": TRACE_B_RAY, "node_B": B_NODE, "tri_B": B_TRI},
+             "counts_per_step": {"rays": radiance, "node_visits": cs.node_visits_trace,
+                                 "tri_tests": cs.tri_tests_trace}}),
+        "k_nee": kernel_roofline(
+            "k_nee (30-try emitter search + bounce)", nee_ms, nee_launches,
+            cs.nee_vertices * NEE_B_VERTEX + cs.shadow_traversals * NEE_B_RAY + cs.node_visits_nee * B_NODE +
+            cs.tri_tests_nee * B_TRI, cs.launches_nee, peak, peak_kind,
+            dram.get("k_nee_dram_bytes_per_vertex"), cs.nee_vertices, dram.get("k_nee_limiter"),
+            {"per_unit": {"vertex_B": NEE_B_VERTEX, "walked_shadow_ray_B": NEE_B_RAY, "node_B": B_NODE,
+                          "tri_B": B_TRI},
+             "counts_per_step": {"nee_vertices": cs.nee_vertices, "shadow_rays": cs.rays_shadow,
+                                 "shadow_traversals": cs.shadow_traversals, "node_visits": cs.node_visits_nee,
+                                 "tri_tests": cs.tri_tests_nee}}),
+    }
+    dominant = max(kernels, key=lambda k: kernels[k]["ms_in_timed_region"])
     rc.close()
     del rc
     # end to end through the C ABI with host buffers: upload + BVH build +
@@ -521,14 +569,9 @@ def run_ours(args, rank, ws, local):
                                                                "probe_mrays_per_s": tuning.mrays_per_s},
                        "l2": "working set > L2 (BVH+triangles+queues) and a 256 MB L2 flush before every step",
                        "bvh": info, "sharding": "disjoint sample ranges per rank"},
-            "roofline": {"bound": "hbm", "kernel": "k_nee (emitter search + bounce)", "achieved": achieved,
-                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": traffic, "bytes_per_launch": nee_bytes_launch,
-                         "avg_launch_ms": avg_nee_s * 1e3,
-                         "per_unit": {"vertex_B": NEE_B_VERTEX, "shadow_ray_B": NEE_B_RAY, "node_B": B_NODE,
-                                      "tri_B": B_TRI},
-                         "counts_per_step": {"nee_vertices": cs.nee_vertices, "shadow_rays": cs.rays_shadow,
-                                             "node_visits": cs.node_visits_nee, "tri_tests": cs.tri_tests_nee}},
+            "roofline": kernels[dominant],
+            "kernels": kernels,
+            "rays_traversed_per_step": (cs.rays_primary + cs.rays_bounce + cs.shadow_traversals),
             "stages_ms_per_step": {"trace": trace_ms / args.steps, "shade": shade_ms / args.steps,
                                    "nee": nee_ms / args.steps, "other": other_ms / args.steps},
             "rays_per_step": rays / args.steps,
