@@ -42,6 +42,26 @@ constexpr uint32_t EMIT_BVH_MIN_TRIS = 32;
 #ifndef LISA_NEE_MIN_BLOCKS
 #define LISA_NEE_MIN_BLOCKS 6  // 6 x 128 threads per SM (80 registers; measured best of 6..8)
 #endif
+// Residency of the closest-hit and shade kernels: blocks per SM the
+// compiler must fit (0 = its own register choice).  Measured: the closest-hit
+// kernel at 8 (64 registers, no spills) is 4 % faster than at 7 (72); the
+// shade kernel is fastest with its own choice (56 registers).
+#ifndef LISA_TRACE_MIN_BLOCKS
+#define LISA_TRACE_MIN_BLOCKS 8
+#endif
+#ifndef LISA_SHADE_MIN_BLOCKS
+#define LISA_SHADE_MIN_BLOCKS 0
+#endif
+#if LISA_TRACE_MIN_BLOCKS > 0
+#define LISA_TRACE_BOUNDS __launch_bounds__(128, LISA_TRACE_MIN_BLOCKS)
+#else
+#define LISA_TRACE_BOUNDS __launch_bounds__(128)
+#endif
+#if LISA_SHADE_MIN_BLOCKS > 0
+#define LISA_SHADE_BOUNDS __launch_bounds__(256, LISA_SHADE_MIN_BLOCKS)
+#else
+#define LISA_SHADE_BOUNDS __launch_bounds__(256)
+#endif
 #ifndef LISA_NEE_PB_MIN_BLOCKS
 #define LISA_NEE_PB_MIN_BLOCKS 7  // physically based emitter kernel: 7 x 128 threads per SM
 #endif
@@ -202,7 +222,7 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
 // and takes the next ray as soon as its own is done (warp-aggregated fetch).
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
+__global__ void LISA_TRACE_BOUNDS k_trace(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->qcount[q];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -263,7 +283,7 @@ __global__ void __launch_bounds__(128) k_trace(WaveBufs b, int depth) {
 // shade: emitter / miss / dielectric / opaque (shader.cu:189-194,211-255)
 
 template <bool PHYS>
-__global__ void __launch_bounds__(256) k_shade(WaveBufs b, int depth) {
+__global__ void LISA_SHADE_BOUNDS k_shade(WaveBufs b, int depth) {
   const int q = depth & 1;
   const uint32_t count = *(volatile uint32_t*)&b.ctrl->qcount[q];
   if (blockIdx.x == 0 && threadIdx.x == 0) b.ctrl->head[HEAD_TRACE] = 0;  // trace of this depth is done
