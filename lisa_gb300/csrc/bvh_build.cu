@@ -415,127 +415,178 @@ __device__ __forceinline__ void sah_child(const SahTree& t, uint32_t c, float4& 
   }
 }
 
-__device__ void treelet_optimize(const SahTree& t, uint32_t root) {
-  uint32_t leaf[TL], inner[TL - 2];
-  float4 llo[TL], lhi[TL];
+// Per-warp shared state of one treelet's restructuring.
+struct TreeletSmem {
+  float opt[1 << TL];        // best SAH cost of each subset of the treelet's leaves
+  uint8_t split[1 << TL];    // its best partition (one side)
+  float4 llo[TL], lhi[TL];   // leaf boxes
   float lcost[TL];
   uint32_t lcnt[TL];
-  int nl = 2, ni = 0;
-  leaf[0] = __ldcg(t.left + root);
-  leaf[1] = __ldcg(t.right + root);
-  sah_child(t, leaf[0], llo[0], lhi[0], lcnt[0], lcost[0]);
-  sah_child(t, leaf[1], llo[1], lhi[1], lcnt[1], lcost[1]);
-  while (nl < TL) {
-    int best = -1;
-    float ba = -1.0f;
-    for (int k = 0; k < nl; ++k) {
-      if (leaf[k] & LEAF_BIT) continue;
-      const float a = box_half_area(llo[k], lhi[k]);
-      if (a > ba) {
-        ba = a;
-        best = k;
+  uint32_t leaf[TL], inner[TL - 2];
+  int nl;
+};
+
+// Treelet restructuring (Karras and Aila, HPG 2013) of the subtree at
+// `root`, by one warp: lane 0 grows the treelet (the largest-area leaf is
+// expanded until TL leaves), the lanes then share the dynamic programme over
+// the subsets of its leaves, one subset size per round (a subset's
+// partitions only use smaller subsets), and lane 0 rebuilds the subtree when
+// the best topology is cheaper.  Every subset's cost is computed by the same
+// operations in the same order as a serial loop would.  All 32 lanes call
+// it with the same root.
+__device__ void treelet_optimize_warp(const SahTree& t, uint32_t root, TreeletSmem& s) {
+  const int lane = threadIdx.x & 31;
+  __syncwarp();  // the root's box, count and cost, just written by its lane, are visible to lane 0
+  if (lane == 0) {
+    int nl = 2, ni = 0;
+    s.leaf[0] = __ldcg(t.left + root);
+    s.leaf[1] = __ldcg(t.right + root);
+    sah_child(t, s.leaf[0], s.llo[0], s.lhi[0], s.lcnt[0], s.lcost[0]);
+    sah_child(t, s.leaf[1], s.llo[1], s.lhi[1], s.lcnt[1], s.lcost[1]);
+    while (nl < TL) {
+      int best = -1;
+      float ba = -1.0f;
+      for (int k = 0; k < nl; ++k) {
+        if (s.leaf[k] & LEAF_BIT) continue;
+        const float a = box_half_area(s.llo[k], s.lhi[k]);
+        if (a > ba) {
+          ba = a;
+          best = k;
+        }
       }
+      if (best < 0) break;
+      const uint32_t c = s.leaf[best];
+      s.inner[ni++] = c;
+      s.leaf[best] = __ldcg(t.left + c);
+      s.leaf[nl] = __ldcg(t.right + c);
+      sah_child(t, s.leaf[best], s.llo[best], s.lhi[best], s.lcnt[best], s.lcost[best]);
+      sah_child(t, s.leaf[nl], s.llo[nl], s.lhi[nl], s.lcnt[nl], s.lcost[nl]);
+      ++nl;
     }
-    if (best < 0) break;
-    const uint32_t c = leaf[best];
-    inner[ni++] = c;
-    leaf[best] = __ldcg(t.left + c);
-    leaf[nl] = __ldcg(t.right + c);
-    sah_child(t, leaf[best], llo[best], lhi[best], lcnt[best], lcost[best]);
-    sah_child(t, leaf[nl], llo[nl], lhi[nl], lcnt[nl], lcost[nl]);
-    ++nl;
+    s.nl = nl;
   }
+  __syncwarp();
+  const int nl = s.nl;
   if (nl < 3) return;  // two leaves have one topology
   const uint32_t full = (1u << nl) - 1u;
-  float opt[1 << TL];
-  uint8_t split[1 << TL];
-  for (uint32_t sset = 1; sset <= full; ++sset) {
+  for (uint32_t sset = lane + 1; sset <= full; sset += 32)
     if ((sset & (sset - 1u)) == 0u) {
-      opt[sset] = lcost[__ffs(sset) - 1];
-      split[sset] = 0;
-      continue;
+      s.opt[sset] = s.lcost[__ffs(sset) - 1];
+      s.split[sset] = 0;
     }
-    float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
-    for (int k = 0; k < nl; ++k)
-      if (sset & (1u << k)) {
-        lo = box_min(lo, llo[k]);
-        hi = box_max(hi, lhi[k]);
+  __syncwarp();
+  for (int size = 2; size <= nl; ++size) {
+    for (uint32_t sset = lane + 1; sset <= full; sset += 32) {
+      if (__popc(sset) != size) continue;
+      float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+      for (int k = 0; k < nl; ++k)
+        if (sset & (1u << k)) {
+          lo = box_min(lo, s.llo[k]);
+          hi = box_max(hi, s.lhi[k]);
+        }
+      const uint32_t low = sset & (0u - sset), rest = sset ^ low;
+      float best = s.opt[low] + s.opt[rest];
+      uint32_t bp = low;
+      // partitions (P, S \ P) with the lowest member in P, each once:
+      // P = low + a nonempty proper subset of the rest
+      for (uint32_t q = (rest - 1u) & rest; q; q = (q - 1u) & rest) {
+        const uint32_t pset = q | low;
+        const float c = s.opt[pset] + s.opt[sset ^ pset];
+        if (c < best) {
+          best = c;
+          bp = pset;
+        }
       }
-    const uint32_t low = sset & (0u - sset), rest = sset ^ low;
-    float best = opt[low] + opt[rest];
-    uint32_t bp = low;
-    // partitions (P, S \ P) with the lowest member in P, each once:
-    // P = low + a nonempty proper subset of the rest
-    for (uint32_t q = (rest - 1u) & rest; q; q = (q - 1u) & rest) {
-      const uint32_t pset = q | low;
-      const float c = opt[pset] + opt[sset ^ pset];
-      if (c < best) {
-        best = c;
-        bp = pset;
-      }
+      s.opt[sset] = SAH_CI * box_half_area(lo, hi) + best;
+      s.split[sset] = (uint8_t)bp;
     }
-    opt[sset] = SAH_CI * box_half_area(lo, hi) + best;
-    split[sset] = (uint8_t)bp;
+    __syncwarp();
   }
-  if (!(opt[full] < __ldcg(t.cost + root) * (1.0f - 1e-6f))) return;  // the present topology is as good
-  // rebuild: the root keeps its id, the other internal subsets reuse inner[]
-  uint32_t st_set[TL], st_node[TL];
-  int sp = 0, next = 0;
-  st_set[sp] = full;
-  st_node[sp++] = root;
-  while (sp) {
-    --sp;
-    const uint32_t sset = st_set[sp], node = st_node[sp];
-    const uint32_t part[2] = {split[sset], sset ^ (uint32_t)split[sset]};
-    uint32_t ch[2];
-    for (int h = 0; h < 2; ++h) {
-      if ((part[h] & (part[h] - 1u)) == 0u) {
-        ch[h] = leaf[__ffs(part[h]) - 1];
-      } else {
-        ch[h] = inner[next++];
-        st_set[sp] = part[h];
-        st_node[sp++] = ch[h];
+  if (lane == 0 && s.opt[full] < __ldcg(t.cost + root) * (1.0f - 1e-6f)) {
+    // rebuild: the root keeps its id, the other internal subsets reuse inner[]
+    uint32_t st_set[TL], st_node[TL];
+    int sp = 0, next = 0;
+    st_set[sp] = full;
+    st_node[sp++] = root;
+    while (sp) {
+      --sp;
+      const uint32_t sset = st_set[sp], node = st_node[sp];
+      const uint32_t part[2] = {s.split[sset], sset ^ (uint32_t)s.split[sset]};
+      uint32_t ch[2];
+      for (int h = 0; h < 2; ++h) {
+        if ((part[h] & (part[h] - 1u)) == 0u) {
+          ch[h] = s.leaf[__ffs(part[h]) - 1];
+        } else {
+          ch[h] = s.inner[next++];
+          st_set[sp] = part[h];
+          st_node[sp++] = ch[h];
+        }
+        if (ch[h] & LEAF_BIT) __stcg(t.parent_leaf + (ch[h] & ~LEAF_BIT), node);
+        else __stcg(t.parent_int + ch[h], node);
       }
-      if (ch[h] & LEAF_BIT) __stcg(t.parent_leaf + (ch[h] & ~LEAF_BIT), node);
-      else __stcg(t.parent_int + ch[h], node);
+      __stcg(t.left + node, ch[0]);
+      __stcg(t.right + node, ch[1]);
+      float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
+      uint32_t cnt = 0;
+      for (int k = 0; k < nl; ++k)
+        if (sset & (1u << k)) {
+          lo = box_min(lo, s.llo[k]);
+          hi = box_max(hi, s.lhi[k]);
+          cnt += s.lcnt[k];
+        }
+      __stcg(t.ilo + node, lo);
+      __stcg(t.ihi + node, hi);
+      __stcg(t.count + node, cnt);
+      __stcg(t.cost + node, s.opt[sset]);
     }
-    __stcg(t.left + node, ch[0]);
-    __stcg(t.right + node, ch[1]);
-    float4 lo = make_float4(3.4e38f, 3.4e38f, 3.4e38f, 0.0f), hi = make_float4(-3.4e38f, -3.4e38f, -3.4e38f, 0.0f);
-    uint32_t cnt = 0;
-    for (int k = 0; k < nl; ++k)
-      if (sset & (1u << k)) {
-        lo = box_min(lo, llo[k]);
-        hi = box_max(hi, lhi[k]);
-        cnt += lcnt[k];
-      }
-    __stcg(t.ilo + node, lo);
-    __stcg(t.ihi + node, hi);
-    __stcg(t.count + node, cnt);
-    __stcg(t.cost + node, opt[sset]);
   }
+  __syncwarp();
 }
 
-__global__ void k_bottom_up_sah(SahTree t, int refine) {
+// Bottom-up pass: boxes, primitive counts and SAH costs of the internal
+// nodes, one leaf per lane climbing to the root; the second lane to reach a
+// node finishes it (the first stops there).  Nodes with enough primitives
+// below are restructured by the whole warp, one lane's node at a time, so
+// the restructuring's dynamic programme runs on 32 lanes.
+constexpr int SAH_THREADS = 256;
+
+__global__ void __launch_bounds__(SAH_THREADS) k_bottom_up_sah(SahTree t, int refine) {
+  __shared__ TreeletSmem tls[SAH_THREADS / 32];
+  TreeletSmem& tl = tls[threadIdx.x >> 5];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.n || t.n < 2) return;
-  uint32_t p = t.parent_leaf[i];
-  while (p != 0xffffffffu) {
-    __threadfence();
-    if (atomicAdd(&t.flags[p], 1u) == 0u) return;
-    __threadfence();
-    float4 a0, a1, b0, b1;
-    uint32_t ca, cb;
-    float sa, sb;
-    sah_child(t, __ldcg(t.left + p), a0, a1, ca, sa);
-    sah_child(t, __ldcg(t.right + p), b0, b1, cb, sb);
-    const float4 lo = box_min(a0, b0), hi = box_max(a1, b1);
-    __stcg(t.ilo + p, lo);
-    __stcg(t.ihi + p, hi);
-    __stcg(t.count + p, ca + cb);
-    __stcg(t.cost + p, SAH_CI * box_half_area(lo, hi) + sa + sb);
-    if (refine && ca + cb >= TREELET_MIN_PRIMS) treelet_optimize(t, p);
-    p = __ldcg(t.parent_int + p);
+  uint32_t p = (i < t.n && t.n >= 2) ? t.parent_leaf[i] : 0xffffffffu;
+  bool active = p != 0xffffffffu;
+  while (__any_sync(0xffffffffu, active)) {
+    bool want = false;
+    if (active) {
+      __threadfence();
+      if (atomicAdd(&t.flags[p], 1u) == 0u) {
+        active = false;
+      } else {
+        __threadfence();
+        float4 a0, a1, b0, b1;
+        uint32_t ca, cb;
+        float sa, sb;
+        sah_child(t, __ldcg(t.left + p), a0, a1, ca, sa);
+        sah_child(t, __ldcg(t.right + p), b0, b1, cb, sb);
+        const float4 lo = box_min(a0, b0), hi = box_max(a1, b1);
+        __stcg(t.ilo + p, lo);
+        __stcg(t.ihi + p, hi);
+        __stcg(t.count + p, ca + cb);
+        __stcg(t.cost + p, SAH_CI * box_half_area(lo, hi) + sa + sb);
+        want = refine && ca + cb >= TREELET_MIN_PRIMS;
+      }
+    }
+    uint32_t m = __ballot_sync(0xffffffffu, want);
+    while (m) {
+      const int owner = __ffs(m) - 1;
+      m &= m - 1;
+      treelet_optimize_warp(t, __shfl_sync(0xffffffffu, p, owner), tl);
+    }
+    if (active) {
+      p = __ldcg(t.parent_int + p);
+      active = p != 0xffffffffu;
+    }
   }
 }
 
@@ -841,7 +892,7 @@ Status build_bvh(const float* d_verts, uint32_t n, cudaStream_t s, ScratchSource
     // boxes, counts and SAH costs bottom up, with treelet restructuring
     // unless refine is off; first/last become count/cost
     const SahTree st{n, vals, plo, phi, par_leaf, par_int, left, right, ilo, ihi, first, (float*)last, flags};
-    k_bottom_up_sah<<<cdiv(n, 256), 256, 0, s>>>(st, refine ? 1 : 0);
+    k_bottom_up_sah<<<cdiv(n, SAH_THREADS), SAH_THREADS, 0, s>>>(st, refine ? 1 : 0);
     LISA_CUDA(cudaGetLastError());
   }
   // outputs
