@@ -272,7 +272,7 @@ Status build_emitter_bvh(Renderer& r, const lisa_renderer_params& p, SceneGpu& s
     emat.push_back(m);
   }
   const uint32_t ne = (uint32_t)gid.size();
-  if (!ne) return Status();
+  if (ne < EMIT_BVH_MIN_TRIS) return Status();  // the emitter search would not use it
   float* d_ev = nullptr;
   int32_t *d_gid = nullptr, *d_emat = nullptr;
   cudaError_t e = cudaMalloc(&d_ev, sizeof(float) * ev.size());

@@ -44,6 +44,9 @@ static_assert(sizeof(DevMaterial) == 48, "DevMaterial layout");
 constexpr float RAY_TMIN = 1e-4f;  // shader.cu:114,202
 constexpr float RAY_TMAX = 1e16f;  // shader.cu:115,202
 constexpr int NEE_TRIES = 30;      // shader.cu:199
+// emissive triangles from which the emitter search uses their own BVH (with
+// fewer, the bounds test of the emitter search is as selective)
+constexpr uint32_t EMIT_BVH_MIN_TRIS = 32;
 constexpr int TRAV_STACK = 64;
 
 enum StatusBits : uint32_t {

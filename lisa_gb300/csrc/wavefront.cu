@@ -36,8 +36,6 @@
 namespace lisa {
 
 constexpr uint32_t FULL = 0xffffffffu;
-// emissive triangles from which the emitter search uses their own BVH
-constexpr uint32_t EMIT_BVH_MIN_TRIS = 32;
 
 #ifndef LISA_NEE_MIN_BLOCKS
 #define LISA_NEE_MIN_BLOCKS 6  // 6 x 128 threads per SM (80 registers; measured best of 6..8)
