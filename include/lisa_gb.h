@@ -103,7 +103,7 @@ typedef struct lisa_options {
   uint32_t mode;             /* LISA_MODE_*                                    */
   uint32_t rng;              /* LISA_RNG_*                                     */
   uint32_t seed;
-  uint32_t paths_in_flight;  /* wavefront size (0 = auto)                      */
+  uint32_t paths_in_flight;  /* wavefront size (0 = 16 Mi; 4 Mi guided)       */
   uint32_t blocks_per_sm;    /* persistent-kernel residency (0 = auto)         */
   uint32_t threads_per_block;/* persistent-kernel block size (0 = auto)        */
   uint32_t use_graph;        /* capture each launch sequence in a CUDA graph   */

@@ -284,7 +284,7 @@ Status autotune(const lisa_renderer_params* scenes, int n, const lisa_options* b
   // training records
   const uint64_t per_path = 156 + (o.mode == LISA_MODE_GUIDED ? 160ull + 80ull * maxd : 0ull);
   std::vector<uint32_t> Ws;
-  for (uint32_t w = 1u << 20; w <= (1u << 23); w <<= 1) {
+  for (uint32_t w = 1u << 20; w <= (1u << 24); w <<= 1) {
     if (w > probe_paths && !Ws.empty()) break;
     if ((uint64_t)w * per_path > free_b / 2 && !Ws.empty()) break;
     Ws.push_back(w);
