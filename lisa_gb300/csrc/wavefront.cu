@@ -206,7 +206,7 @@ __global__ void k_raygen(WaveBufs b, const WaveDesc* __restrict__ wave) {
       dir = normalize(focus - org);
     }
     b.ro[0][slot] = make_float4(org.x, org.y, org.z, __uint_as_float(slot));
-    b.rd[0][slot] = make_float4(dir.x, dir.y, dir.z, RAY_TMAX);
+    b.rd[0][slot] = make_float4(dir.x, dir.y, dir.z, __uint_as_float(g.scene));
     // w: the stale emitter flag (compat, -1 = none) or the pdf of the last
     // diffuse bounce (physically based, 0 = camera or specular)
     b.ps_att[slot] = make_float4(1.0f, 1.0f, 1.0f, b.physical ? 0.0f : __int_as_float(-1));
@@ -255,9 +255,8 @@ __global__ void LISA_TRACE_BOUNDS k_trace(WaveBufs b, int depth) {
           ray = base + __popc(nmask & lt);
           if (ray < count) {
             const float4 o = b.ro[q][ray], d = b.rd[q][ray];
-            const uint32_t slot = __float_as_uint(o.w);
-            ts = trace_scene(b.scenes[__float_as_uint(b.ps_col[slot].w) >> 24]);
-            active = trav_begin(s, ts, ld3(o), ld3(d), RAY_TMIN, d.w);
+            ts = trace_scene(b.scenes[__float_as_uint(d.w)]);
+            active = trav_begin(s, ts, ld3(o), ld3(d), RAY_TMIN, RAY_TMAX);
             if (!active) b.hit[ray] = make_int2(-1, 0x7f800000);
           } else {
             exhausted = true;
@@ -294,19 +293,21 @@ __global__ void LISA_SHADE_BOUNDS k_shade(WaveBufs b, int depth) {
     V3 p = v3(0.0f), nd = v3(0.0f), N = v3(0.0f), d = v3(0.0f);
     uint32_t slot = 0;
     int mat_idx = 0;
+    uint32_t scene = 0;
     if (i < count) {
       const int2 h = b.hit[i];
       const float4 o4 = b.ro[q][i];
+      const float4 d4 = b.rd[q][i];
       slot = __float_as_uint(o4.w);
+      scene = __float_as_uint(d4.w);
       if (h.x >= 0) {  // a miss adds the background, 0 (optix_wrapper.cc:354-356), and ends the path
-        const float4 col = b.ps_col[slot];
-        const uint32_t scene = __float_as_uint(col.w) >> 24;
         const SceneDev& sc = b.scenes[scene];
         mat_idx = prim_material(sc, h.x);
         const DevMaterial& m = sc.mats[mat_idx];
         float4 att = b.ps_att[slot];
         if (m.cls == MAT_EMIT) {
           // color += Le * att; done (shader.cu:216-218)
+          const float4 col = b.ps_col[slot];
           V3 le = v3(m.emission[0], m.emission[1], m.emission[2]) * ld3(att);
           if (PHYS && att.w > 0.0f) {
             // reached by a diffuse bounce: power-heuristic weight against
@@ -317,7 +318,7 @@ __global__ void LISA_SHADE_BOUNDS k_shade(WaveBufs b, int depth) {
             const V3 v0 = ld3(pr[0]);
             const V3 cr = cross3(ld3(pr[1]) - v0, ld3(pr[2]) - v0);
             const V3 n = cr * fdiv(1.0f, fsqrt(dot(cr, cr)));
-            const float cos_y = fabsf(dot(n, ld3(b.rd[q][i])));
+            const float cos_y = fabsf(dot(n, ld3(d4)));
             float w = 0.0f;
             if (cos_y > 0.0f) {
               const float pl = fdiv(fmul(m.light_pdf, fmul(t, t)), cos_y);
@@ -330,7 +331,6 @@ __global__ void LISA_SHADE_BOUNDS k_shade(WaveBufs b, int depth) {
         } else if (!PHYS || depth < (int)sc.num_bounces) {
           // (physically based: the ray leaving the last vertex only gathers
           // the emission it reaches, so any other hit ends the path)
-          const float4 d4 = b.rd[q][i];
           d = ld3(d4);
           const float t = __int_as_float(h.y);
           p = ld3(o4) + t * d;
@@ -387,13 +387,13 @@ __global__ void LISA_SHADE_BOUNDS k_shade(WaveBufs b, int depth) {
     const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
     if (want_ray && queue_fits(b, ri)) {
       b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
-      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, __uint_as_float(scene));
     }
     const uint32_t ni = warp_reserve(&b.ctrl->nee_count, want_nee);
     if (want_nee && queue_fits(b, ni)) {
       b.nee_a[ni] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
       b.nee_b[ni] = make_float4(N.x, N.y, N.z, __int_as_float(mat_idx));
-      b.nee_c[ni] = make_float4(d.x, d.y, d.z, 0.0f);
+      b.nee_c[ni] = make_float4(d.x, d.y, d.z, __uint_as_float(scene));
     }
   }
 }
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
       const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
       if (want_ray && queue_fits(b, ri)) {
         b.ro[q ^ 1][ri] = make_float4(s.r.ox, s.r.oy, s.r.oz, __uint_as_float(slot));
-        b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+        b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((uint32_t)(sc - b.scenes)));
       }
       const bool need = !have && !exhausted;
       const uint32_t nmask = __ballot_sync(FULL, need);
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
             mat_idx = __float_as_int(b4.w);
             stale = __float_as_int(b.ps_att[slot].w);
             seed = b.ps_rng[slot];
-            sc = b.scenes + (__float_as_uint(b.ps_col[slot].w) >> 24);
+            sc = b.scenes + __float_as_uint(__ldg(&b.nee_c[entry].w));
             ts = trace_scene(*sc);
             tries = 0;
             have = true;
@@ -689,11 +689,12 @@ __device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, uint32
 // new direction, over the throughput after the bounce, is the incident
 // radiance).  Returns whether a continuation ray (p, nd) is wanted.
 __device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int depth, uint32_t i, const float* o, V3& p,
-                                                     V3& nd, uint32_t& slot, uint32_t& guided_n) {
+                                                     V3& nd, uint32_t& slot, uint32_t& scene, uint32_t& guided_n) {
   const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
   slot = __float_as_uint(a4.w);
   const float4 cw = b.ps_col[slot];
-  const SceneDev& sc = b.scenes[__float_as_uint(cw.w) >> 24];
+  scene = __float_as_uint(cw.w) >> 24;
+  const SceneDev& sc = b.scenes[scene];
   if (sc.mats[__float_as_int(b4.w)].roughness != 1.0f) return false;  // bounced in k_nee
   p = ld3(a4);
   const V3 N = ld3(b4);
@@ -794,7 +795,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
       const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want_ray);
       if (want_ray && queue_fits(b, ri)) {
         b.ro[q ^ 1][ri] = make_float4(s.r.ox, s.r.oy, s.r.oz, __uint_as_float(slot));
-        b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+        b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, __uint_as_float((uint32_t)(sc - b.scenes)));
       }
       const bool need = !have && !exhausted;
       const uint32_t nmask = __ballot_sync(FULL, need);
@@ -815,9 +816,10 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
             const V3 N = ld3(b4);
             mat_idx = __float_as_int(b4.w);
             seed = b.ps_rng[slot];
-            sc = b.scenes + (__float_as_uint(b.ps_col[slot].w) >> 24);
+            const float4 c4 = b.nee_c[entry];
+            sc = b.scenes + __float_as_uint(c4.w);
             ts = trace_scene(*sc);
-            Ns = dot(N, ld3(b.nee_c[entry])) < 0.0f ? N : -N;  // faces the incoming ray
+            Ns = dot(N, ld3(c4)) < 0.0f ? N : -N;  // faces the incoming ray
             have = true;
             shadow = false;
             wi = v3(0.0f);
@@ -872,7 +874,7 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
 // mixture, q = c cos/pi + (1-c) q_guide, throughput x (cos/pi) / q -- with a
 // training record per diffuse bounce.
 __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, uint32_t i, const float* o, V3& p,
-                                                 V3& nd, uint32_t& slot, uint32_t& guided_n) {
+                                                 V3& nd, uint32_t& slot, uint32_t& scene, uint32_t& guided_n) {
   const float c = b.bsdf_fraction;
   const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
   p = ld3(a4);
@@ -881,7 +883,8 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
   const V3 D = ld3(b.nee_c[i]);
   const V3 Ns = dot(N, D) < 0.0f ? N : -N;
   const float4 cw = b.ps_col[slot];
-  const SceneDev& sc = b.scenes[__float_as_uint(cw.w) >> 24];
+  scene = __float_as_uint(cw.w) >> 24;
+  const SceneDev& sc = b.scenes[scene];
   const float r = sc.mats[__float_as_int(b4.w)].roughness;
   V3 att = ld3(b.ps_att[slot]);
   V3 col = ld3(cw);
@@ -941,15 +944,15 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
   infer_tiles<SRC_NEE>(pack, master, src, status, [&](uint32_t i, bool valid, const float* o) {
     bool want = false;
     V3 p = v3(0.0f), nd = v3(0.0f);
-    uint32_t slot = 0;
+    uint32_t slot = 0, scene = 0;
     if (valid) {
-      if (PHYS) want = guided_pb_vertex(b, depth, i, o, p, nd, slot, guided_n);
-      else want = guided_compat_vertex(b, depth, i, o, p, nd, slot, guided_n);
+      if (PHYS) want = guided_pb_vertex(b, depth, i, o, p, nd, slot, scene, guided_n);
+      else want = guided_compat_vertex(b, depth, i, o, p, nd, slot, scene, guided_n);
     }
     const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want);
     if (want && queue_fits(b, ri)) {
       b.ro[q ^ 1][ri] = make_float4(p.x, p.y, p.z, __uint_as_float(slot));
-      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, RAY_TMAX);
+      b.rd[q ^ 1][ri] = make_float4(nd.x, nd.y, nd.z, __uint_as_float(scene));
     }
   });
   warp_add32(&b.ctrl->guided_count, guided_n);

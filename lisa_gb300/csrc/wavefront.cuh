@@ -9,14 +9,15 @@ namespace lisa {
 // Structure-of-arrays wavefront state.  A "slot" is one path in flight.
 struct WaveBufs {
   float4* ro[2];    // ray queues (ping-pong): origin xyz, w = slot
-  float4* rd[2];    //                          direction xyz, w = tmax
+  float4* rd[2];    //                          direction xyz, w = scene index (bits; every
+                    //                          queued ray runs to RAY_TMAX)
   int2* hit;        // closest hit per queued ray: (triangle, t bits)
   float4* ps_att;   // per slot: throughput xyz, w = stale emitter material (int, -1 none)
   float4* ps_col;   // per slot: radiance xyz,  w = scene<<24 | pixel
   uint32_t* ps_rng; // per slot: LCG state
   float4* nee_a;    // emitter-search queue: hit point xyz, w = slot
   float4* nee_b;    //                       shading normal xyz, w = material
-  float4* nee_c;    //                       incoming direction xyz, w unused
+  float4* nee_c;    //                       incoming direction xyz, w = scene index (bits)
   WaveCtrl* ctrl;
   const SceneDev* scenes;
   uint32_t capacity;
