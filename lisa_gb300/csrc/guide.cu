@@ -10,12 +10,18 @@
 // K = 16 per instruction) and commits to an mbarrier; waits are bounded and
 // a time-out sets a status bit instead of hanging.
 //
-// Backward of layer l (weights W_l: out x in):
-//   dH_{l-1} = dZ_l W_l          A = dZ_l tile [b][o] (K = o), B = W_l^T rows
-//   dW_l    += dZ_l^T H_{l-1}    A = [dZ_l^T ; H_{l-1}^T] (M = 128, K = batch),
-//                                B = H_{l-1}^T; rows 0..63 of D are dW_l
-// dW accumulates in TMEM across all tiles of the CTA and is added to the
-// global FP32 gradient once at the end.
+// Backward of layer l (weights W_l: out x in; its input H_{l-1} is
+// activation tile l, rows = samples):
+//   dH_{l-1} = dZ_l W_l          A = dZ_l tile [b][o] (K-major, K = o),
+//                                B = W_l^T rows
+//   dW_l    += dZ_l^T H_{l-1}    A = [H_{l-1}^T ; dZ_l^T] (M = 128, K = batch),
+//                                B = H_{l-1}^T; rows 64..127 of D are dW_l
+// dW reads the row-per-sample tiles as MN-major operands, so nothing is
+// transposed: dZ_l is written to tile l + 1 (dead by then: its last reader
+// was the ReLU mask of layer l + 1), one 16 KB tile after H_{l-1}, which is
+// the stride between A's two 64-row blocks.  dW accumulates in TMEM across
+// all tiles of the CTA and is added to the global FP32 gradient once at the
+// end.
 #include <cmath>
 #include <cstring>
 #include <random>
@@ -135,7 +141,7 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guide_infer(const 
                                                                           const float* __restrict__ master,
                                                                           GuideSrc src, float* __restrict__ out,
                                                                           uint32_t* status) {
-  infer_tiles<SRC>(pack, master, src, status, [&](uint32_t i, bool valid, const float* o) {
+  infer_tiles<SRC>(pack, master, src, status, [](uint32_t) {}, [&](uint32_t i, bool valid, const float* o) {
     if (!valid) return;
     float4* d = reinterpret_cast<float4*>(out + 40ull * i);
 #pragma unroll
@@ -147,18 +153,17 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guide_infer(const 
 // training: grads += d loss / d params, loss += sum of the per-sample losses
 
 constexpr int TILE = 16384;
-constexpr int TRAIN_OFF_ACT = PACK_BYTES;              // X, H1..H4
-constexpr int TRAIN_OFF_DZ = TRAIN_OFF_ACT + 5 * TILE;  // dZ tile [b][o]
-constexpr int TRAIN_OFF_AT = TRAIN_OFF_DZ + TILE;       // [dZ^T ; H^T], two K halves
-constexpr int TRAIN_SMEM_USED = TRAIN_OFF_AT + 2 * TILE;
-constexpr int TRAIN_SMEM = TRAIN_SMEM_USED + 1024 + 16384;
+// tiles X, H1..H4 (tile l = the input of layer l), a sixth tile for dZ of
+// the output layer, and a seventh that no step writes: the dW steps of the
+// output layer read at most 32 KB past the start of tile 4 (two 1024-byte
+// K atoms and two 64-row blocks, whichever of the descriptor's two strides
+// the hardware takes for which), so every operand read stays inside the
+// allocation
+constexpr int TRAIN_OFF_ACT = PACK_BYTES;
+constexpr int TRAIN_SMEM_USED = TRAIN_OFF_ACT + 7 * TILE;
+constexpr int TRAIN_SMEM = TRAIN_SMEM_USED + 1024 + 2048;  // manual 1024-B alignment, slack
 static_assert(TRAIN_SMEM <= 227 * 1024, "training kernel shared memory");
 constexpr uint32_t TM_FWD = 0, TM_DH = 64, TM_DW = 128;  // TMEM columns; dW_l at 128 + 64 l
-
-// element (m, b) of the transposed operand: two K halves of [128 x 64]
-__device__ __forceinline__ uint32_t at_offset(uint32_t m, uint32_t b) {
-  return (b >> 6) * (uint32_t)TILE + tc::sw128_offset(m, b & 63u);
-}
 
 // One halving round of a warp reduce-scatter: the lane keeps the upper or
 // lower half of its n values (by lane bit m) plus the partner's same half.
@@ -199,9 +204,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
-  uint8_t* act = smem + TRAIN_OFF_ACT;  // tile l = H_l (H_0 = X)
-  uint8_t* dzt = smem + TRAIN_OFF_DZ;
-  uint8_t* at = smem + TRAIN_OFF_AT;
+  uint8_t* act = smem + TRAIN_OFF_ACT;  // tile l = the input of layer l (tile 0 = X)
   __shared__ uint64_t mbar;
   __shared__ uint64_t mbar_w;  // the packed weights' bulk copy
   __shared__ uint32_t tmem_base;
@@ -293,16 +296,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
       if (failed) break;
       if (l < 4) {
         tc::tmem_ld16x<4>(tmem + TM_FWD + lane_off, v);
-        const float4* bb = reinterpret_cast<const float4*>(s_b + 64 * l);
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const float4 b4 = bb[q];
-          v[4 * q] = fmaxf(v[4 * q] + b4.x, 0.0f);
-          v[4 * q + 1] = fmaxf(v[4 * q + 1] + b4.y, 0.0f);
-          v[4 * q + 2] = fmaxf(v[4 * q + 2] + b4.z, 0.0f);
-          v[4 * q + 3] = fmaxf(v[4 * q + 3] + b4.w, 0.0f);
-        }
-        store_row_bf16(act + (l + 1) * TILE, tid, v);
+        store_row_bias_relu(act + (l + 1) * TILE, tid, v, s_b + 64 * l);
       } else {
         tc::tmem_ld16x<3>(tmem + TM_FWD + lane_off, v);
       }
@@ -332,32 +326,26 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
     add_bias_grad(s_db + 4 * 64, g, 40);
     // backward, layer 5 (index 4) down to layer 1 (index 0)
     for (int l = 4; l >= 0 && !failed; --l) {
-      // dZ_l (registers g) -> dZ tile (A of dH) and dZ^T rows of AT;
-      // H_{l-1} (tile l) -> H^T rows of AT
-      store_row_bf16(dzt, tid, g);
-      {
-        float h[64];
-        load_row_bf16(act + l * TILE, tid, h);
-#pragma unroll 8
-        for (int k = 0; k < 64; ++k) {
-          *(uint16_t*)(at + at_offset((uint32_t)k, (uint32_t)tid)) = f2bf(g[k]);
-          *(uint16_t*)(at + at_offset((uint32_t)(64 + k), (uint32_t)tid)) = f2bf(h[k]);
-        }
-      }
+      // dZ_l (registers g) -> tile l + 1: A of dH (K-major) and the upper
+      // 64-row block of A of dW (MN-major)
+      uint8_t* tl = act + l * TILE;
+      store_row_bf16(tl + TILE, tid, g);
       sync_for_mma();
       if (tid == 0) {
-        // dW_l += [dZ^T ; H^T] x (H^T)^T over the 128 samples (K = 128)
-        const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
-        const uint32_t sat = tc::smem_u32(at);
+        // dW_l += [H^T ; dZ^T] x (H^T)^T over the 128 samples (K = 128):
+        // both operands MN-major, 16 samples (two 8-row atoms) per step
+        const uint32_t idesc_mn = tc::idesc_bf16_f32_mn(128, 64);
+        const uint32_t sh = tc::smem_u32(tl);
 #pragma unroll
         for (uint32_t ks = 0; ks < 8; ++ks) {
-          const uint32_t base = sat + (ks >> 2) * TILE + (ks & 3) * 32;
-          tc::mma_bf16(tmem + TM_DW + 64 * l, tc::sw128_desc(base), tc::sw128_desc(base + 64 * 128), idesc,
+          const uint32_t base = sh + ks * 2048;
+          tc::mma_bf16(tmem + TM_DW + 64 * l, tc::sw128_mn_desc(base, TILE), tc::sw128_mn_desc(base, TILE), idesc_mn,
                        (first && ks == 0) ? 0u : 1u);
         }
         if (l > 0) {
           // dH_{l-1} = dZ_l W_l  (B = W_l^T rows)
-          const uint32_t sdz = tc::smem_u32(dzt), swt = tc::smem_u32(w + (R_T + 64 * (l - 1)) * 128);
+          const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
+          const uint32_t sdz = sh + TILE, swt = tc::smem_u32(w + (R_T + 64 * (l - 1)) * 128);
 #pragma unroll
           for (uint32_t k = 0; k < 4; ++k)
             tc::mma_bf16(tmem + TM_DH, tc::sw128_desc(sdz + 32 * k), tc::sw128_desc(swt + 32 * k), idesc, k);
@@ -367,24 +355,33 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
       wait_mma();
       if (failed) break;
       if (l > 0) {
-        float h[64];
-        load_row_bf16(act + l * TILE, tid, h);
+        // dZ_{l-1} = dH_{l-1} where H_{l-1} > 0: the BF16 bits of this
+        // sample's row of tile l, +-0 masked out
         tc::tmem_ld16x<4>(tmem + TM_DH + lane_off, g);
 #pragma unroll
-        for (int k = 0; k < 64; ++k) g[k] = h[k] > 0.0f ? g[k] : 0.0f;
+        for (int c = 0; c < 8; ++c) {
+          const uint4 q = *(const uint4*)(tl + tid * 128 + ((c ^ (tid & 7)) << 4));
+          const uint32_t hw[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if ((hw[j] & 0x7fffu) == 0u) g[8 * c + 2 * j] = 0.0f;
+            if ((hw[j] & 0x7fff0000u) == 0u) g[8 * c + 2 * j + 1] = 0.0f;
+          }
+        }
         add_bias_grad(s_db + 64 * (l - 1), g, 64);
       }
       tc::fence_before_sync();
     }
     first = false;
   }
-  // flush: dW rows 0..63 live in TMEM lanes of warps 0 and 1
+  // flush: dW (rows 64..127 of the accumulators) lives in the TMEM lanes of
+  // warps 2 and 3
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const bool ok = !failed && !first;
-  if (warp < 2) {
-    const int o = warp * 32 + (tid & 31);
+  if (warp >= 2) {
+    const int o = (warp - 2) * 32 + (tid & 31);
     for (int l = 0; l < 5; ++l) {
       const int rows = l < 4 ? 64 : 40;
       float d[64];

@@ -69,6 +69,21 @@ __device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, flo
   }
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Brings sample i's feature rows into L2 ahead of load_features (emitter
+// queue only: the other sources stream in order).
+template <int SRC>
+__device__ __forceinline__ void prefetch_features(const GuideSrc& s, uint32_t i) {
+  if (SRC == SRC_NEE) {
+    prefetch_l2(s.nee_a + i);
+    prefetch_l2(s.nee_b + i);
+    prefetch_l2(s.nee_c + i);
+  }
+}
+
 // Writes 64 values as BF16 (round to nearest even) into row `row` of a
 // swizzled tile, two values per conversion.
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
@@ -87,16 +102,29 @@ __device__ __forceinline__ void store_row_bf16(uint8_t* tile, int row, const flo
   }
 }
 
-__device__ __forceinline__ void load_row_bf16(const uint8_t* tile, int row, float* v) {
+// relu(lo + blo), relu(hi + bhi) as BF16x2: one packed FP32 add (add.rn.f32x2,
+// the same rounding as two scalar adds) and one converting ReLU
+// (cvt.rn.relu.bf16x2.f32: negative sums become +0).
+__device__ __forceinline__ uint32_t bias_relu_bf16x2(float lo, float hi, float blo, float bhi) {
+  const float2 s = __fadd2_rn(make_float2(lo, hi), make_float2(blo, bhi));
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(s.y), "f"(s.x));  // first source -> upper half
+  return d;
+}
+
+// Row `row` of a hidden layer's output tile: relu(acc + bias) as BF16 (the
+// bias is 64 FP32 values in shared memory, 16-byte aligned).
+__device__ __forceinline__ void store_row_bias_relu(uint8_t* tile, int row, const float* acc, const float* bias) {
+  const float4* b4 = reinterpret_cast<const float4*>(bias);
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
-    const uint4 q = *(const uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4));
-    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      v[8 * c + 2 * j] = bf2f((uint16_t)(w[j] & 0xffffu));
-      v[8 * c + 2 * j + 1] = bf2f((uint16_t)(w[j] >> 16));
-    }
+    const float4 u = b4[2 * c], w = b4[2 * c + 1];
+    uint4 q;
+    q.x = bias_relu_bf16x2(acc[8 * c + 0], acc[8 * c + 1], u.x, u.y);
+    q.y = bias_relu_bf16x2(acc[8 * c + 2], acc[8 * c + 3], u.z, u.w);
+    q.z = bias_relu_bf16x2(acc[8 * c + 4], acc[8 * c + 5], w.x, w.y);
+    q.w = bias_relu_bf16x2(acc[8 * c + 6], acc[8 * c + 7], w.z, w.w);
+    *(uint4*)(tile + row * 128 + ((c ^ (row & 7)) << 4)) = q;
   }
 }
 
@@ -127,20 +155,22 @@ constexpr int INFER_BLOCKS_PER_SM = 3;
 // Runs the network on samples [src.first, n) and calls
 // epi(i, valid, o) in every thread for its sample i of each tile (valid =
 // i < n; o = the 40 outputs, bias included).  All 128 threads call epi
-// together, so it may use warp-collective operations.  Needs INFER_SMEM
-// bytes of dynamic shared memory and 128 threads.
+// together, so it may use warp-collective operations.  pre(i) runs for
+// each valid sample when its features are loaded, five layers before its
+// epi: a place to start the epilogue's memory traffic (prefetches).  Needs
+// INFER_SMEM bytes of dynamic shared memory and 128 threads.
 //
 // Two tiles are in flight per CTA: while the threads run the epilogue of one
 // tile's layer (TMEM -> bias, ReLU -> BF16 rows), the tensor core runs the
 // other tile's layer.  A layer's output overwrites its input tile in shared
 // memory: the MMA that read it has completed when the epilogue starts.
-template <int SRC, class Epi>
+template <int SRC, class Pre, class Epi>
 __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, const float* __restrict__ master,
-                                            const GuideSrc& src, uint32_t* status, Epi&& epi) {
+                                            const GuideSrc& src, uint32_t* status, Pre&& pre, Epi&& epi) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
-  uint8_t* act[2] = {smem + FWD_BYTES, smem + FWD_BYTES + 16384};
+  uint8_t* const act0 = smem + FWD_BYTES;  // tile k at act0 + k * 16384
   __shared__ uint64_t mbar[2];
   __shared__ uint64_t mbar_w;  // the packed weights' bulk copy
   __shared__ uint32_t tmem_base;
@@ -171,29 +201,38 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
   const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-  // thread 0's view of the two barriers: parity of the next completion, and
-  // whether a committed MMA has not been waited for
-  uint32_t phase[2] = {0, 0};
-  bool busy[2] = {false, false};
+  // thread 0's view of the two barriers, one bit per tile: parity of the
+  // next completion, and whether a committed MMA has not been waited for
+  // (bit masks rather than arrays indexed by the tile, which would live in
+  // local memory)
+  uint32_t phase = 0, busy = 0;
   auto weights = [&](int l) { return w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128; };
   auto issue = [&](int k, int l) {
-    issue_layer(tmem + 64u * k, act[k], weights(l), l < 4 ? 64u : 48u, &mbar[k]);
-    busy[k] = true;
+    issue_layer(tmem + 64u * k, act0 + 16384 * k, weights(l), l < 4 ? 64u : 48u, &mbar[k]);
+    busy |= 1u << k;
   };
   for (uint32_t t0 = 2 * blockIdx.x; t0 < ntiles && !failed; t0 += 2 * gridDim.x) {
     const int nt = t0 + 1 < ntiles ? 2 : 1;  // tiles of this pair (uniform over the block)
-    uint32_t idx[2];
+    const uint32_t idx0 = src.first + t0 * 128 + tid;  // this thread's sample in tile k: idx0 + 128 k
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      idx[k] = src.first + (t0 + k) * 128 + tid;
+      const uint32_t i = idx0 + 128 * k;
       if (k < nt) {
         float f[64];
-        if (idx[k] < n) load_features<SRC>(src, idx[k], f);
-        else
+        if (i < n) {
+          load_features<SRC>(src, i, f);
+          pre(i);
+        } else
 #pragma unroll
           for (int q = 0; q < 64; ++q) f[q] = 0.0f;
-        store_row_bf16(act[k], tid, f);
+        store_row_bf16(act0 + 16384 * k, tid, f);
       }
+    }
+    // the next pair's feature rows, while this pair runs
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const uint32_t j = src.first + (t0 + 2 * gridDim.x + k) * 128 + tid;
+      if (j < n) prefetch_features<SRC>(src, j);
     }
     tc::fence_smem_async();
     tc::fence_before_sync();
@@ -206,9 +245,9 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
 #pragma unroll 1
       for (int k = 0; k < nt; ++k) {
         if (tid == 0) {
-          if (tc::mbar_wait(&mbar[k], phase[k])) {
-            phase[k] ^= 1;
-            busy[k] = false;
+          if (tc::mbar_wait(&mbar[k], (phase >> k) & 1u)) {
+            phase ^= 1u << k;
+            busy &= ~(1u << k);
           } else {
             atomicOr(status, ST_GUIDE_NONFINITE << 1);
             failed = 1;
@@ -221,16 +260,7 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
         float acc[64];
         if (l < 4) {
           tc::tmem_ld16x<4>(lane_addr, acc);
-          const float4* bb = reinterpret_cast<const float4*>(s_bias + 64 * l);
-#pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const float4 b4 = bb[q];
-            acc[4 * q] = fmaxf(acc[4 * q] + b4.x, 0.0f);
-            acc[4 * q + 1] = fmaxf(acc[4 * q + 1] + b4.y, 0.0f);
-            acc[4 * q + 2] = fmaxf(acc[4 * q + 2] + b4.z, 0.0f);
-            acc[4 * q + 3] = fmaxf(acc[4 * q + 3] + b4.w, 0.0f);
-          }
-          store_row_bf16(act[k], tid, acc);  // H_l over H_{l-1}
+          store_row_bias_relu(act0 + 16384 * k, tid, acc, s_bias + 64 * l);  // H_l over H_{l-1}
           tc::fence_smem_async();
           tc::fence_before_sync();
           __syncthreads();
@@ -240,7 +270,8 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
           tc::tmem_ld16x<3>(lane_addr, acc);
 #pragma unroll
           for (int q = 0; q < 40; ++q) acc[q] += s_bias[4 * 64 + q];
-          epi(idx[k], idx[k] < n, acc);
+          const uint32_t i = idx0 + 128 * k;
+          epi(i, i < n, acc);
           tc::fence_before_sync();
         }
       }
@@ -255,7 +286,7 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   // before their TMEM is freed
   if (tid == 0) {
     for (int k = 0; k < 2; ++k)
-      if (busy[k]) tc::mbar_wait(&mbar[k], phase[k], 1u << 20);
+      if ((busy >> k) & 1u) tc::mbar_wait(&mbar[k], (phase >> k) & 1u, 1u << 20);
     if (failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy
   }
   tc::fence_before_sync();

@@ -114,17 +114,18 @@ __device__ __forceinline__ float mix_pdf(const Lobe* L, float wx, float wy, floa
 // Sample the mixture with three uniforms in [0,1).
 __device__ __forceinline__ void mix_sample(const Lobe* L, float u0, float u1, float u2, float& wx, float& wy,
                                            float& wz) {
-  int j = LOBES - 1;
+  // the first lobe whose cumulative weight exceeds u0 (the last one if
+  // none does), picked by selects so that L stays in registers
+  Lobe l = L[LOBES - 1];
   float acc = 0.0f;
+  bool found = false;
 #pragma unroll
-  for (int k = 0; k < LOBES; ++k) {
+  for (int k = 0; k < LOBES - 1; ++k) {
     acc += L[k].w;
-    if (u0 < acc) {
-      j = k;
-      break;
-    }
+    const bool take = !found && u0 < acc;
+    if (take) l = L[k];
+    found = found || take;
   }
-  const Lobe& l = L[j];
   const float k = l.kappa;
   // cos of the angle to mu: 1 + log(u1 + (1-u1) e^{-2k}) / k  (kappa <= e^5
   // keeps e^{-2k} representable enough; the clamp guards u1 = 0)

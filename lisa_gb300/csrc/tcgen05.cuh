@@ -38,6 +38,22 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
+// UMMA shared-memory descriptor, MN-major, 128-byte swizzle: the same tile
+// image read the other way round.  Each 128-byte row holds 64 consecutive
+// M (or N) elements of one K index; 8 rows (8 K indices) form a 1024-byte
+// swizzle atom, so the stride byte offset (between 8-row K groups) is
+// 1024 B and the leading byte offset is the stride between 64-element
+// blocks along M (or N).  One K = 16 step spans two atoms (2048 B).
+__device__ __forceinline__ uint64_t sw128_mn_desc(uint32_t saddr, uint32_t mn_block_stride) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((mn_block_stride & 0x3FFFFu) >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
 // Instruction descriptor of kind::f16 with BF16 A and B (both K-major) and
 // an FP32 accumulator, shape M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
@@ -46,6 +62,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
          | (1u << 10)         // B format BF16
          | ((N >> 3) << 17)   // N / 8
          | ((M >> 4) << 24);  // M / 16
+}
+
+// The same with A and B both MN-major (transpose bits 15 and 16).
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_mn(uint32_t M, uint32_t N) {
+  return idesc_bf16_f32(M, N) | (1u << 15) | (1u << 16);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.

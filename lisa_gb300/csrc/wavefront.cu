@@ -941,7 +941,15 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
                                                                            int depth) {
   const int q = depth & 1;
   uint32_t guided_n = 0;
-  infer_tiles<SRC_NEE>(pack, master, src, status, [&](uint32_t i, bool valid, const float* o) {
+  // the path state and emitter sample that the guided bounce reads, brought
+  // into L2 while the five layers run
+  auto pre = [&](uint32_t i) {
+    const uint32_t slot = __float_as_uint(b.nee_a[i].w);
+    prefetch_l2(b.ps_col + slot);
+    prefetch_l2(b.ps_rng + slot);
+    if (PHYS) prefetch_l2(b.nee_light + 2ull * i);
+  };
+  infer_tiles<SRC_NEE>(pack, master, src, status, pre, [&](uint32_t i, bool valid, const float* o) {
     bool want = false;
     V3 p = v3(0.0f), nd = v3(0.0f);
     uint32_t slot = 0, scene = 0;

@@ -63,6 +63,8 @@ def main(argv=None):
                           "mrays_per_s": st.rays / max(st.ms_device, 1e-9) / 1e3,
                           "stages_ms": {"trace": st.ms_trace, "shade": st.ms_shade, "nee": st.ms_nee,
                                         "guide": st.ms_guide, "other": st.ms_other},
+                          "guide_infer": {"ms": st.ms_guide_infer, "rows": st.guide_infer_rows},
+                          "guide_train": {"ms": st.ms_guide_train, "samples": st.guide_train_samples},
                           "launches": st.launches_total, "status": st.device_status}), flush=True)
     r.close()
 
