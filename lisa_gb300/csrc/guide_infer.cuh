@@ -63,9 +63,10 @@ __device__ __forceinline__ void load_features(const GuideSrc& s, uint32_t i, flo
     const float4 a = s.nee_a[i], b = s.nee_b[i], c = s.nee_c[i];
     // view direction: towards where the ray came from
     const float il = rsqrtf(fmaxf(c.x * c.x + c.y * c.y + c.z * c.z, 1e-30f));
-    const int stale = __float_as_int(s.ps_att[__float_as_uint(a.w)].w);
-    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il,
-                  (stale >= 0 && !s.no_flag) ? 1.0f : 0.0f, f);
+    // the emitter flag (path state, a random access) only where it is a feature
+    const bool flag = !s.no_flag && __float_as_int(s.ps_att[__float_as_uint(a.w)].w) >= 0;
+    guide::encode(s.bmin, s.bmax, a.x, a.y, a.z, b.x, b.y, b.z, -c.x * il, -c.y * il, -c.z * il, flag ? 1.0f : 0.0f,
+                  f);
   }
 }
 

@@ -653,13 +653,14 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
 }
 
 // Appends the training record of a guided vertex with probability
-// 1 - drop_prob (decided by a hash of slot, depth and the wave's salt, not
-// by the path's stream), warp-aggregated over the lanes that call it.
-__device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, uint32_t slot, float flag, float4 r0,
-                                            float4 r1, float4 r2, float4 r3, V3 c0) {
+// 1 - drop (decided by a hash of slot, depth and the wave's salt, not by the
+// path's stream; drop = ctrl->drop_prob, read once per launch), warp-aggregated
+// over the lanes that call it.
+__device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, float drop, uint32_t slot, float flag,
+                                            float4 r0, float4 r1, float4 r2, float4 r3, V3 c0) {
   if (b.rec_cap == 0) return;  // a wave that does not train keeps no records
   const float u = (float)(tea<4>(slot * 16u + (uint32_t)depth, b.rec_salt) >> 8) * (1.0f / 16777216.0f);
-  const bool keep = u >= b.ctrl->drop_prob;
+  const bool keep = u >= drop;
   const uint32_t active = __activemask();
   const uint32_t mask = __ballot_sync(active, keep);
   if (!mask) return;
@@ -688,17 +689,18 @@ __device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, uint32
 // with a training record per vertex (the radiance later gathered along the
 // new direction, over the throughput after the bounce, is the incident
 // radiance).  Returns whether a continuation ray (p, nd) is wanted.
-__device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int depth, uint32_t i, const float* o, V3& p,
-                                                     V3& nd, uint32_t& slot, uint32_t& scene, uint32_t& guided_n) {
-  const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
+__device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int depth, float drop, uint32_t i,
+                                                     const float* o, V3& p, V3& nd, uint32_t& slot, uint32_t& scene,
+                                                     uint32_t& guided_n) {
+  const float4 a4 = b.nee_a[i], b4 = b.nee_b[i], c4 = b.nee_c[i];
   slot = __float_as_uint(a4.w);
-  const float4 cw = b.ps_col[slot];
-  scene = __float_as_uint(cw.w) >> 24;
+  scene = __float_as_uint(c4.w);
   const SceneDev& sc = b.scenes[scene];
   if (sc.mats[__float_as_int(b4.w)].roughness != 1.0f) return false;  // bounced in k_nee
+  const float4 cw = b.ps_col[slot];
   p = ld3(a4);
   const V3 N = ld3(b4);
-  const V3 D = ld3(b.nee_c[i]);
+  const V3 D = ld3(c4);
   uint32_t seed = b.ps_rng[slot];
   const float4 at = b.ps_att[slot];
   const int stale = __float_as_int(at.w);
@@ -706,7 +708,7 @@ __device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int dept
   nd = guided_bounce(o, N, seed, b.bsdf_fraction, weight);
   const V3 att = ld3(at) * weight;
   const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-  keep_record(b, depth, slot, stale >= 0 ? 1.0f : 0.0f, make_float4(p.x, p.y, p.z, weight),
+  keep_record(b, depth, drop, slot, stale >= 0 ? 1.0f : 0.0f, make_float4(p.x, p.y, p.z, weight),
               make_float4(N.x, N.y, N.z, nd.x), make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y),
               make_float4(att.x, att.y, att.z, nd.z), ld3(cw));
   b.ps_rng[slot] = seed;
@@ -873,17 +875,17 @@ __global__ void __launch_bounds__(128, LISA_NEE_PB_MIN_BLOCKS) k_nee_pb(WaveBufs
 // one-sample MIS between cosine sampling (probability c) and the guide's
 // mixture, q = c cos/pi + (1-c) q_guide, throughput x (cos/pi) / q -- with a
 // training record per diffuse bounce.
-__device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, uint32_t i, const float* o, V3& p,
-                                                 V3& nd, uint32_t& slot, uint32_t& scene, uint32_t& guided_n) {
+__device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, float drop, uint32_t i, const float* o,
+                                                 V3& p, V3& nd, uint32_t& slot, uint32_t& scene, uint32_t& guided_n) {
   const float c = b.bsdf_fraction;
-  const float4 a4 = b.nee_a[i], b4 = b.nee_b[i];
+  const float4 a4 = b.nee_a[i], b4 = b.nee_b[i], c4 = b.nee_c[i];
   p = ld3(a4);
   slot = __float_as_uint(a4.w);
+  scene = __float_as_uint(c4.w);
   const V3 N = ld3(b4);
-  const V3 D = ld3(b.nee_c[i]);
+  const V3 D = ld3(c4);
   const V3 Ns = dot(N, D) < 0.0f ? N : -N;
   const float4 cw = b.ps_col[slot];
-  scene = __float_as_uint(cw.w) >> 24;
   const SceneDev& sc = b.scenes[scene];
   const float r = sc.mats[__float_as_int(b4.w)].roughness;
   V3 att = ld3(b.ps_att[slot]);
@@ -917,7 +919,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, u
     prev = r * qm;
     want = weight > 0.0f;
     const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-    keep_record(b, depth, slot, 0.0f, make_float4(p.x, p.y, p.z, weight), make_float4(N.x, N.y, N.z, nd.x),
+    keep_record(b, depth, drop, slot, 0.0f, make_float4(p.x, p.y, p.z, weight), make_float4(N.x, N.y, N.z, nd.x),
                 make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y), make_float4(att.x, att.y, att.z, nd.z), col);
     ++guided_n;
   } else {
@@ -941,6 +943,7 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
                                                                            int depth) {
   const int q = depth & 1;
   uint32_t guided_n = 0;
+  const float drop = b.ctrl->drop_prob;  // written by the last wave's record collection
   // the path state and emitter sample that the guided bounce reads, brought
   // into L2 while the five layers run
   auto pre = [&](uint32_t i) {
@@ -954,8 +957,8 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
     V3 p = v3(0.0f), nd = v3(0.0f);
     uint32_t slot = 0, scene = 0;
     if (valid) {
-      if (PHYS) want = guided_pb_vertex(b, depth, i, o, p, nd, slot, scene, guided_n);
-      else want = guided_compat_vertex(b, depth, i, o, p, nd, slot, scene, guided_n);
+      if (PHYS) want = guided_pb_vertex(b, depth, drop, i, o, p, nd, slot, scene, guided_n);
+      else want = guided_compat_vertex(b, depth, drop, i, o, p, nd, slot, scene, guided_n);
     }
     const uint32_t ri = warp_reserve(&b.ctrl->qcount[q ^ 1], want);
     if (want && queue_fits(b, ri)) {

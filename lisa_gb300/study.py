@@ -118,7 +118,9 @@ def batch(args) -> List[dict]:
         res[name] = dict(ms=st.ms_device, wall_s=wall, rays=st.rays, mrays_per_s=st.rays / st.ms_device / 1e3,
                          launches=st.launches_total, tuning=tune.as_dict(),
                          stages_ms={"trace": st.ms_trace, "shade": st.ms_shade, "nee": st.ms_nee,
-                                    "guide": st.ms_guide, "other": st.ms_other})
+                                    "guide": st.ms_guide, "other": st.ms_other},
+                         guide_infer={"ms": st.ms_guide_infer, "rows": st.guide_infer_rows},
+                         guide_train={"ms": st.ms_guide_train, "samples": st.guide_train_samples})
         imgs[name] = [r.image(k) for k in range(len(params))]
         r.close()
     # per-scene reference: ref_mult x the spp, plain, FP64
@@ -194,6 +196,10 @@ def summary_md(rows: List[dict], cmd: str) -> str:
                 lines.append(f"| {m} | {x['ms']:.1f} | {x['mrays_per_s']:.0f} | {x['launches']} | "
                              f"W={t['paths_in_flight']}, {t['threads_per_block']} thr, refill {t['refill_idle']} | "
                              + ", ".join(f"{k} {v:.0f}" for k, v in sm.items()) + " |")
+            gi, gt = r["guided"].get("guide_infer"), r["guided"].get("guide_train")
+            if gi and gt:
+                lines += ["", f"Guide in the guided batch: inference {gi['ms']:.0f} ms over {gi['rows']:,} vertices, "
+                              f"training {gt['ms']:.0f} ms over {gt['samples']:,} samples."]
             lines += ["", f"Median over scenes of guided equal-time relMSE / plain relMSE, every scene "
                           f"charged the batch-wide time ratio {r['guided']['ms'] / r['plain']['ms']:.3f}: "
                           f"{r['median_equal_time_ratio']:.3f}", ""]
