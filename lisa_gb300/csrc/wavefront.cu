@@ -652,25 +652,32 @@ __global__ void __launch_bounds__(128, LISA_NEE_MIN_BLOCKS) k_nee(WaveBufs b, in
   }
 }
 
-// Appends the training record of a guided vertex with probability
-// 1 - drop (decided by a hash of slot, depth and the wave's salt, not by the
-// path's stream; drop = ctrl->drop_prob, read once per launch), warp-aggregated
-// over the lanes that call it.
-__device__ __forceinline__ void keep_record(const WaveBufs& b, int depth, float drop, uint32_t slot, float flag,
-                                            float4 r0, float4 r1, float4 r2, float4 r3, V3 c0) {
-  if (b.rec_cap == 0) return;  // a wave that does not train keeps no records
+// Training records of guided vertices, in two halves so that the slot's
+// atomic is in flight while the vertex is finished.  record_reserve keeps a
+// vertex's record with probability 1 - drop (decided by a hash of slot,
+// depth and the wave's salt, not by the path's stream; drop =
+// ctrl->drop_prob, read once per launch), warp-aggregated over the lanes
+// that call it, and returns the record index or ~0u; record_write fills it.
+__device__ __forceinline__ uint32_t record_reserve(const WaveBufs& b, int depth, float drop, uint32_t slot,
+                                                   bool want) {
+  if (b.rec_cap == 0) return ~0u;  // a wave that does not train keeps no records
   const float u = (float)(tea<4>(slot * 16u + (uint32_t)depth, b.rec_salt) >> 8) * (1.0f / 16777216.0f);
-  const bool keep = u >= drop;
+  const bool keep = want && u >= drop;
   const uint32_t active = __activemask();
   const uint32_t mask = __ballot_sync(active, keep);
-  if (!mask) return;
+  if (!mask) return ~0u;
   const int leader = __ffs(mask) - 1;
   const int lane = threadIdx.x & 31;
   uint32_t base = 0;
   if (lane == leader) base = atomicAdd(&b.ctrl->rec_count, (uint32_t)__popc(mask));
   base = __shfl_sync(active, base, leader);
   const uint32_t k = base + __popc(mask & lanemask_lt());
-  if (!keep || k >= b.rec_cap) return;
+  return keep && k < b.rec_cap ? k : ~0u;
+}
+
+__device__ __forceinline__ void record_write(const WaveBufs& b, uint32_t k, uint32_t slot, float flag, float4 r0,
+                                             float4 r1, float4 r2, float4 r3, V3 c0) {
+  if (k == ~0u) return;
   float4* rec = b.rec_list + 5ull * k;
   rec[0] = r0;
   rec[1] = r1;
@@ -697,6 +704,7 @@ __device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int dept
   scene = __float_as_uint(c4.w);
   const SceneDev& sc = b.scenes[scene];
   if (sc.mats[__float_as_int(b4.w)].roughness != 1.0f) return false;  // bounced in k_nee
+  const uint32_t rk = record_reserve(b, depth, drop, slot, true);
   const float4 cw = b.ps_col[slot];
   p = ld3(a4);
   const V3 N = ld3(b4);
@@ -708,7 +716,7 @@ __device__ __forceinline__ bool guided_compat_vertex(const WaveBufs& b, int dept
   nd = guided_bounce(o, N, seed, b.bsdf_fraction, weight);
   const V3 att = ld3(at) * weight;
   const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-  keep_record(b, depth, drop, slot, stale >= 0 ? 1.0f : 0.0f, make_float4(p.x, p.y, p.z, weight),
+  record_write(b, rk, slot, stale >= 0 ? 1.0f : 0.0f, make_float4(p.x, p.y, p.z, weight),
               make_float4(N.x, N.y, N.z, nd.x), make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y),
               make_float4(att.x, att.y, att.z, nd.z), ld3(cw));
   b.ps_rng[slot] = seed;
@@ -891,6 +899,11 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, f
   V3 att = ld3(b.ps_att[slot]);
   V3 col = ld3(cw);
   uint32_t seed = b.ps_rng[slot];
+  // the lobe choice is the stream's first draw at this vertex, as when the
+  // bounce is drawn in k_nee_pb; decided first so that the training
+  // record's slot is reserved while the mixture is evaluated
+  const bool diffuse = r >= 1.0f || (r > 0.0f && rnd(seed) < r);
+  const uint32_t rk = record_reserve(b, depth, drop, slot, diffuse);
   guide::Lobe L[guide::LOBES];
   guide::decode(o, L);
   const float4 l0 = b.nee_light[2ull * i], l1 = b.nee_light[2ull * i + 1];
@@ -904,7 +917,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, f
   }
   float prev = 0.0f;
   bool want;
-  if (r >= 1.0f || (r > 0.0f && rnd(seed) < r)) {
+  if (diffuse) {
     if (rnd(seed) < c) {
       nd = cosine_dir(Ns, seed);
     } else {
@@ -919,7 +932,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, f
     prev = r * qm;
     want = weight > 0.0f;
     const float il = rsqrtf(fmaxf(dot(D, D), 1e-30f));
-    keep_record(b, depth, drop, slot, 0.0f, make_float4(p.x, p.y, p.z, weight), make_float4(N.x, N.y, N.z, nd.x),
+    record_write(b, rk, slot, 0.0f, make_float4(p.x, p.y, p.z, weight), make_float4(N.x, N.y, N.z, nd.x),
                 make_float4(-D.x * il, -D.y * il, -D.z * il, nd.y), make_float4(att.x, att.y, att.z, nd.z), col);
     ++guided_n;
   } else {
@@ -950,7 +963,10 @@ __global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const
     const uint32_t slot = __float_as_uint(b.nee_a[i].w);
     prefetch_l2(b.ps_col + slot);
     prefetch_l2(b.ps_rng + slot);
-    if (PHYS) prefetch_l2(b.nee_light + 2ull * i);
+    if (PHYS) {
+      prefetch_l2(b.ps_att + slot);  // (the reference estimator's flag feature has loaded it)
+      prefetch_l2(b.nee_light + 2ull * i);
+    }
   };
   infer_tiles<SRC_NEE>(pack, master, src, status, pre, [&](uint32_t i, bool valid, const float* o) {
     bool want = false;
