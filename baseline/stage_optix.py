@@ -103,8 +103,8 @@ def nvcc_ptx(src: str, out: str, fast_math: bool = True) -> None:
 
 
 def main() -> None:
-    ref = os.environ.get("LISA_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src", "LiSA")):
+    ref = os.environ.get("LISA_REFERENCE_DIR", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "src", "LiSA")):
         sys.exit(f"reference tree not found at {ref} (set LISA_REFERENCE_DIR)")
     if os.path.isdir(OUT):
         shutil.rmtree(OUT)
