@@ -137,7 +137,7 @@ __global__ void k_guide_reduce(const float* __restrict__ part, const float* __re
 }
 
 template <int SRC>
-__global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guide_infer(const uint16_t* __restrict__ pack,
+__global__ void __launch_bounds__(INFER_THREADS, INFER_BLOCKS_PER_SM) k_guide_infer(const uint16_t* __restrict__ pack,
                                                                           const float* __restrict__ master,
                                                                           GuideSrc src, float* __restrict__ out,
                                                                           uint32_t* status) {
@@ -512,9 +512,9 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
   const uint32_t pairs = std::max<uint32_t>(1, (max_n + 255) / 256);  // two tiles of 128 per CTA
   const uint32_t grid = std::min<uint32_t>(pairs, (uint32_t)sm_count_current() * INFER_BLOCKS_PER_SM);
   if (src_kind == SRC_RAW)
-    k_guide_infer<SRC_RAW><<<grid, 128, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
+    k_guide_infer<SRC_RAW><<<grid, INFER_THREADS, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
   else
-    k_guide_infer<SRC_NEE><<<grid, 128, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
+    k_guide_infer<SRC_NEE><<<grid, INFER_THREADS, INFER_SMEM, s>>>(g.w_bf16, g.master, src, out, g.status);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }

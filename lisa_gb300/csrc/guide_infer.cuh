@@ -147,37 +147,44 @@ __device__ __forceinline__ uint8_t* align1024(uint8_t* p) {
 // inference: the five layers, tile by tile
 
 // + 1024 for the manual 1024-byte alignment, + 2 KB of slack after the last
-// operand tile.  Three CTAs share an SM (3 x 75.8 KB of shared memory,
-// 3 x 128 TMEM columns, <= 168 registers a thread), each with two tiles in
-// flight.
+// operand tile.  A CTA is two warpgroups sharing one copy of the weights,
+// each with its own tile, accumulator (64 TMEM columns), mbarrier and MMA
+// thread; two CTAs share an SM (2 x 74.8 KB of shared memory, 2 x 128 TMEM
+// columns, <= 128 registers a thread): 16 warps and four tile pipelines per
+// SM.
 constexpr int INFER_SMEM = FWD_BYTES + 2 * 16384 + 1024 + 2048;
-constexpr int INFER_BLOCKS_PER_SM = 3;
+constexpr int INFER_THREADS = 256;
+constexpr int INFER_BLOCKS_PER_SM = 2;
 
-// Runs the network on samples [src.first, n) and calls
-// epi(i, valid, o) in every thread for its sample i of each tile (valid =
-// i < n; o = the 40 outputs, bias included).  All 128 threads call epi
-// together, so it may use warp-collective operations.  pre(i) runs for
-// each valid sample when its features are loaded, five layers before its
-// epi: a place to start the epilogue's memory traffic (prefetches).  Needs
-// INFER_SMEM bytes of dynamic shared memory and 128 threads.
+// Runs the network on samples [src.first, n) and calls epi(i, valid, o) in
+// the 128 threads of a warpgroup for their samples i of each tile (valid =
+// i < n; o = the 40 outputs, bias included); epi may use warp-collective
+// operations.  pre(i) runs for each valid sample when its features are
+// loaded, five layers before its epi: a place to start the epilogue's
+// memory traffic (prefetches).  Needs INFER_SMEM bytes of dynamic shared
+// memory and INFER_THREADS threads.
 //
-// Two tiles are in flight per CTA: while the threads run the epilogue of one
-// tile's layer (TMEM -> bias, ReLU -> BF16 rows), the tensor core runs the
-// other tile's layer.  A layer's output overwrites its input tile in shared
-// memory: the MMA that read it has completed when the epilogue starts.
+// The two warpgroups of a CTA run independent pipelines (named barriers,
+// one per warpgroup): thread 0 of a warpgroup issues its tile's layer
+// (tcgen05.mma, M = 128, K = 16 per instruction) and waits for it on the
+// warpgroup's mbarrier; the warpgroup meets at its barrier, every thread
+// reads its accumulator row with tcgen05.ld and writes the next layer's
+// input row (bias, ReLU, BF16) over the tile in shared memory.  While one
+// warpgroup runs an epilogue, the tensor core runs the other warpgroups'
+// layers.
 template <int SRC, class Pre, class Epi>
 __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, const float* __restrict__ master,
                                             const GuideSrc& src, uint32_t* status, Pre&& pre, Epi&& epi) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
-  uint8_t* const act0 = smem + FWD_BYTES;  // tile k at act0 + k * 16384
-  __shared__ uint64_t mbar[2];
-  __shared__ uint64_t mbar_w;  // the packed weights' bulk copy
+  __shared__ uint64_t mbar[2];  // one per warpgroup
+  __shared__ uint64_t mbar_w;   // the packed weights' bulk copy
   __shared__ uint32_t tmem_base;
-  __shared__ int failed;
+  __shared__ int failed[2];     // per warpgroup
+  __shared__ int weights_failed;
   __shared__ __align__(16) float s_bias[4 * 64 + 48];
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, wg = tid >> 7, t = tid & 127;
   // samples [src.first, n)
   const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
   const uint32_t ntiles = (n - src.first + 127) / 128;
@@ -188,112 +195,98 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
     tc::mbar_init(&mbar_w, 1);
     tc::fence_mbar_init();
     tc::bulk_load(w, pack, FWD_BYTES, &mbar_w);  // weights by TMA while the rest is set up
-    failed = 0;
+    failed[0] = failed[1] = 0;
+    weights_failed = 0;
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
-  for (int k = tid; k < 4 * 64 + 48; k += 128) s_bias[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
+  for (int k = tid; k < 4 * 64 + 48; k += INFER_THREADS) s_bias[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
   if (tid == 0 && !tc::mbar_wait(&mbar_w, 0)) {
     atomicOr(status, ST_GUIDE_NONFINITE << 1);
-    failed = 1;
+    failed[0] = failed[1] = 1;
+    weights_failed = 1;
   }
   tc::fence_smem_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tmem = tmem_base;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-  // thread 0's view of the two barriers, one bit per tile: parity of the
-  // next completion, and whether a committed MMA has not been waited for
-  // (bit masks rather than arrays indexed by the tile, which would live in
-  // local memory)
-  uint32_t phase = 0, busy = 0;
-  auto weights = [&](int l) { return w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128; };
-  auto issue = [&](int k, int l) {
-    issue_layer(tmem + 64u * k, act0 + 16384 * k, weights(l), l < 4 ? 64u : 48u, &mbar[k]);
-    busy |= 1u << k;
+  const uint32_t tmem = tmem_base + 64u * wg;  // this warpgroup's accumulator columns
+  const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  uint8_t* const act = smem + FWD_BYTES + 16384 * wg;
+  const uint32_t bar_id = 1u + wg;
+  auto wg_sync = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(bar_id) : "memory"); };
+  // thread 0 of the warpgroup: parity of the next completion, and whether a
+  // committed MMA has not been waited for
+  uint32_t phase = 0;
+  bool busy = false;
+  auto issue = [&](int l) {
+    issue_layer(tmem, act, w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, l < 4 ? 64u : 48u, &mbar[wg]);
+    busy = true;
   };
-  for (uint32_t t0 = 2 * blockIdx.x; t0 < ntiles && !failed; t0 += 2 * gridDim.x) {
-    const int nt = t0 + 1 < ntiles ? 2 : 1;  // tiles of this pair (uniform over the block)
-    const uint32_t idx0 = src.first + t0 * 128 + tid;  // this thread's sample in tile k: idx0 + 128 k
+  for (uint32_t tile = 2 * blockIdx.x + wg; tile < ntiles; tile += 2 * gridDim.x) {
+    if (failed[wg]) break;  // read after a warpgroup barrier: uniform over the warpgroup
+    const uint32_t i = src.first + tile * 128 + t;
+    {
+      float f[64];
+      if (i < n) {
+        load_features<SRC>(src, i, f);
+        pre(i);
+      } else {
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const uint32_t i = idx0 + 128 * k;
-      if (k < nt) {
-        float f[64];
-        if (i < n) {
-          load_features<SRC>(src, i, f);
-          pre(i);
-        } else
-#pragma unroll
-          for (int q = 0; q < 64; ++q) f[q] = 0.0f;
-        store_row_bf16(act0 + 16384 * k, tid, f);
+        for (int q = 0; q < 64; ++q) f[q] = 0.0f;
       }
+      store_row_bf16(act, t, f);
     }
-    // the next pair's feature rows, while this pair runs
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const uint32_t j = src.first + (t0 + 2 * gridDim.x + k) * 128 + tid;
-      if (j < n) prefetch_features<SRC>(src, j);
-    }
+    // the warpgroup's next tile's feature rows, while this one runs
+    const uint32_t j = src.first + (tile + 2 * gridDim.x) * 128 + t;
+    if (j < n) prefetch_features<SRC>(src, j);
     tc::fence_smem_async();
     tc::fence_before_sync();
-    __syncthreads();
+    wg_sync();
     tc::fence_after_sync();
-    if (tid == 0)
-      for (int k = 0; k < nt; ++k) issue(k, 0);
+    if (t == 0) issue(0);
 #pragma unroll 1
     for (int l = 0; l < 5; ++l) {
-#pragma unroll 1
-      for (int k = 0; k < nt; ++k) {
-        if (tid == 0) {
-          if (tc::mbar_wait(&mbar[k], (phase >> k) & 1u)) {
-            phase ^= 1u << k;
-            busy &= ~(1u << k);
-          } else {
-            atomicOr(status, ST_GUIDE_NONFINITE << 1);
-            failed = 1;
-          }
-        }
-        __syncthreads();  // the others learn of the finished MMA here
-        tc::fence_after_sync();
-        if (failed) break;
-        const uint32_t lane_addr = tmem + 64u * k + lane_off;
-        float acc[64];
-        if (l < 4) {
-          tc::tmem_ld16x<4>(lane_addr, acc);
-          store_row_bias_relu(act0 + 16384 * k, tid, acc, s_bias + 64 * l);  // H_l over H_{l-1}
-          tc::fence_smem_async();
-          tc::fence_before_sync();
-          __syncthreads();
-          tc::fence_after_sync();
-          if (tid == 0) issue(k, l + 1);
+      if (t == 0) {
+        if (tc::mbar_wait(&mbar[wg], phase)) {
+          phase ^= 1u;
+          busy = false;
         } else {
-          tc::tmem_ld16x<3>(lane_addr, acc);
-#pragma unroll
-          for (int q = 0; q < 40; ++q) acc[q] += s_bias[4 * 64 + q];
-          const uint32_t i = idx0 + 128 * k;
-          epi(i, i < n, acc);
-          tc::fence_before_sync();
+          atomicOr(status, ST_GUIDE_NONFINITE << 1);
+          failed[wg] = 1;
         }
       }
-      if (failed) break;
+      wg_sync();  // the others learn of the finished MMA here
+      tc::fence_after_sync();
+      if (failed[wg]) break;
+      float acc[64];
+      if (l < 4) {
+        tc::tmem_ld16x<4>(lane_addr, acc);
+        store_row_bias_relu(act, t, acc, s_bias + 64 * l);  // H_l over H_{l-1}
+        tc::fence_smem_async();
+        tc::fence_before_sync();
+        wg_sync();
+        tc::fence_after_sync();
+        if (t == 0) issue(l + 1);
+      } else {
+        tc::tmem_ld16x<3>(lane_addr, acc);
+#pragma unroll
+        for (int q = 0; q < 40; ++q) acc[q] += s_bias[4 * 64 + q];
+        epi(i, i < n, acc);
+      }
     }
-    // the next pair rewrites both tiles and both accumulators
+    // the next tile rewrites the tile and the accumulator
     tc::fence_before_sync();
-    __syncthreads();
+    wg_sync();
     tc::fence_after_sync();
   }
-  // after a time-out, give MMAs still in flight a bounded chance to finish
-  // before their TMEM is freed
-  if (tid == 0) {
-    for (int k = 0; k < 2; ++k)
-      if ((busy >> k) & 1u) tc::mbar_wait(&mbar[k], (phase >> k) & 1u, 1u << 20);
-    if (failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy
-  }
+  // after a time-out, give an MMA still in flight a bounded chance to finish
+  // before its TMEM is freed
+  if (t == 0 && busy) tc::mbar_wait(&mbar[wg], phase, 1u << 20);
+  if (tid == 0 && weights_failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tmem, 128);
+  if (warp == 0) tc::tmem_dealloc(tmem_base, 128);
 }
 
 }  // namespace lisa

@@ -950,7 +950,7 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, f
 // guided bounces of those vertices (tensor-core layers, guide_infer.cuh;
 // bounce in the last layer's epilogue).
 template <bool PHYS>
-__global__ void __launch_bounds__(128, INFER_BLOCKS_PER_SM) k_guided_infer(const uint16_t* __restrict__ pack,
+__global__ void __launch_bounds__(INFER_THREADS, INFER_BLOCKS_PER_SM) k_guided_infer(const uint16_t* __restrict__ pack,
                                                                            const float* __restrict__ master,
                                                                            GuideSrc src, uint32_t* status, WaveBufs b,
                                                                            int depth) {
@@ -1454,10 +1454,10 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
           if (!waves[wv].train) bw.rec_cap = 0;
           const uint32_t grid = std::min<uint32_t>((r.capacity + 255) / 256, (uint32_t)(r.sm_count * INFER_BLOCKS_PER_SM));
           if (physical)
-            k_guided_infer<true><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
+            k_guided_infer<true><<<grid, INFER_THREADS, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
                                                                        bw, (int)d);
           else
-            k_guided_infer<false><<<grid, 128, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
+            k_guided_infer<false><<<grid, INFER_THREADS, INFER_SMEM, r.stream>>>(net->w_bf16, net->master, infer_src, net->status,
                                                                         bw, (int)d);
           return Status();
         }));
