@@ -195,6 +195,161 @@ __device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int c
   if (col + 1 < count) atomicAdd(&s_db[col + 1], e[1]);
 }
 
+// Forward, loss gradient and backward of one 128-sample tile (thread t owns
+// sample i = row t): dW accumulates in TMEM (initialised by the first tile
+// of a batch), db and the loss in shared memory.  The caller has the weights
+// (w) and biases (s_b) in shared memory and has met at a barrier since.
+template <int SRC>
+__device__ __forceinline__ void train_tile(const GuideSrc& src, uint32_t i, uint32_t n, float inv_n, uint8_t* w,
+                                           uint8_t* act, uint32_t tmem, uint32_t lane_off, uint64_t* mbar,
+                                           uint32_t& phase, bool first, volatile int* failed, uint32_t* status,
+                                           const float* s_b, float* s_db, float* s_loss) {
+  const int tid = threadIdx.x;
+  auto wait_mma = [&]() {
+    if (tid == 0 && !tc::mbar_wait(mbar, phase)) {
+      atomicOr(status, ST_GUIDE_NONFINITE << 1);
+      *failed = 1;
+    }
+    phase ^= 1;
+    __syncthreads();
+    tc::fence_after_sync();
+  };
+  auto sync_for_mma = [&]() {
+    tc::fence_smem_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+  };
+  const bool valid = i < n;
+  float v[64];
+  float wx = 0.0f, wy = 0.0f, wz = 1.0f, wt = 0.0f;
+  if (valid) {
+    load_features<SRC>(src, i, v);
+    if (SRC == SRC_RAW) {
+      wx = __ldg(src.dirs + 3ull * i);
+      wy = __ldg(src.dirs + 3ull * i + 1);
+      wz = __ldg(src.dirs + 3ull * i + 2);
+      wt = __ldg(src.weights + i);
+    } else {
+      const float4 c = src.geom[4ull * i + 2], d = src.geom[4ull * i + 3];
+      wx = c.y;
+      wy = c.z;
+      wz = c.w;
+      wt = d.x;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 64; ++k) v[k] = 0.0f;
+  }
+  store_row_bf16(act, tid, v);
+  // forward
+  for (int l = 0; l < 5; ++l) {
+    sync_for_mma();
+    const uint32_t N = l < 4 ? 64u : 48u;
+    if (tid == 0) issue_layer(tmem + TM_FWD, act + l * TILE, w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, N, mbar);
+    wait_mma();
+    if (*failed) return;
+    if (l < 4) {
+      tc::tmem_ld16x<4>(tmem + TM_FWD + lane_off, v);
+      store_row_bias_relu(act + (l + 1) * TILE, tid, v, s_b + 64 * l);
+    } else {
+      tc::tmem_ld16x<3>(tmem + TM_FWD + lane_off, v);
+    }
+    tc::fence_before_sync();
+  }
+  // loss gradient at the output (40 values, padded with zeros to 64)
+  float g[64];
+  {
+    float o[40];
+#pragma unroll
+    for (int k = 0; k < 40; ++k) o[k] = v[k] + s_b[4 * 64 + k];
+    float lsum = 0.0f;
+    if (valid && wt != 0.0f) {
+      const float il = rsqrtf(fmaxf(wx * wx + wy * wy + wz * wz, 1e-30f));
+      lsum = guide::loss_grad(o, wx * il, wy * il, wz * il, wt * inv_n, g);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 40; ++k) g[k] = 0.0f;
+    }
+#pragma unroll
+    for (int k = 40; k < 64; ++k) g[k] = 0.0f;
+#pragma unroll
+    for (int o2 = 16; o2 > 0; o2 >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o2);
+    if ((tid & 31) == 0) atomicAdd(s_loss, lsum);
+  }
+  add_bias_grad(s_db + 4 * 64, g, 40);
+  // backward, layer 5 (index 4) down to layer 1 (index 0)
+  for (int l = 4; l >= 0; --l) {
+    // dZ_l (registers g) -> tile l + 1: A of dH (K-major) and the upper
+    // 64-row block of A of dW (MN-major)
+    uint8_t* tl = act + l * TILE;
+    store_row_bf16(tl + TILE, tid, g);
+    sync_for_mma();
+    if (tid == 0) {
+      // dW_l += [H^T ; dZ^T] x (H^T)^T over the 128 samples (K = 128):
+      // both operands MN-major, 16 samples (two 8-row atoms) per step
+      const uint32_t idesc_mn = tc::idesc_bf16_f32_mn(128, 64);
+      const uint32_t sh = tc::smem_u32(tl);
+#pragma unroll
+      for (uint32_t ks = 0; ks < 8; ++ks) {
+        const uint32_t base = sh + ks * 2048;
+        tc::mma_bf16(tmem + TM_DW + 64 * l, tc::sw128_mn_desc(base, TILE), tc::sw128_mn_desc(base, TILE), idesc_mn,
+                     (first && ks == 0) ? 0u : 1u);
+      }
+      if (l > 0) {
+        // dH_{l-1} = dZ_l W_l  (B = W_l^T rows)
+        const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
+        const uint32_t sdz = sh + TILE, swt = tc::smem_u32(w + (R_T + 64 * (l - 1)) * 128);
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k)
+          tc::mma_bf16(tmem + TM_DH, tc::sw128_desc(sdz + 32 * k), tc::sw128_desc(swt + 32 * k), idesc, k);
+      }
+      tc::mma_commit(mbar);
+    }
+    wait_mma();
+    if (*failed) return;
+    if (l > 0) {
+      // dZ_{l-1} = dH_{l-1} where H_{l-1} > 0: the BF16 bits of this
+      // sample's row of tile l, +-0 masked out
+      tc::tmem_ld16x<4>(tmem + TM_DH + lane_off, g);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const uint4 q = *(const uint4*)(tl + tid * 128 + ((c ^ (tid & 7)) << 4));
+        const uint32_t hw[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if ((hw[j] & 0x7fffu) == 0u) g[8 * c + 2 * j] = 0.0f;
+          if ((hw[j] & 0x7fff0000u) == 0u) g[8 * c + 2 * j + 1] = 0.0f;
+        }
+      }
+      add_bias_grad(s_db + 64 * (l - 1), g, 64);
+    }
+    tc::fence_before_sync();
+  }
+}
+
+// Reads this thread's row o (< 64) of dW_l, l = 0..4 (rows 64..127 of the
+// accumulators: the TMEM lanes of warps 2 and 3), and hands each layer's
+// row to put(l, o, d) when the layer has that row (W5 has 40).
+template <class Put>
+__device__ __forceinline__ void flush_dw(uint32_t tmem, uint32_t lane_off, bool ok, Put&& put) {
+  const int warp = threadIdx.x >> 5;
+  if (warp < 2) return;
+  const int o = (warp - 2) * 32 + (threadIdx.x & 31);
+  for (int l = 0; l < 5; ++l) {
+    const int rows = l < 4 ? 64 : 40;
+    float d[64];
+    if (ok) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DW + 64 * l + lane_off + c * 16, d + c * 16);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 64; ++c) d[c] = 0.0f;
+    }
+    if (o < rows) put(l, o, d);
+  }
+}
+
 template <int SRC>
 __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restrict__ pack, const float* __restrict__ master,
                                                         GuideSrc src, float inv_n, float* __restrict__ part,
@@ -248,161 +403,200 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
   uint32_t phase = 0;
   bool first = true;
-  auto wait_mma = [&]() {
-    if (!tc::mbar_wait(&mbar, phase)) {
-      atomicOr(status, ST_GUIDE_NONFINITE << 1);
-      failed = 1;
-    }
-    phase ^= 1;
-    tc::fence_after_sync();
-    __syncthreads();
-  };
-  auto sync_for_mma = [&]() {
-    tc::fence_smem_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-  };
   for (uint32_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
-    const uint32_t i = src.first + t * 128 + tid;
-    const bool valid = i < n;
-    float v[64];
-    float wx = 0.0f, wy = 0.0f, wz = 1.0f, wt = 0.0f;
-    if (valid) {
-      load_features<SRC>(src, i, v);
-      if (SRC == SRC_RAW) {
-        wx = __ldg(src.dirs + 3ull * i);
-        wy = __ldg(src.dirs + 3ull * i + 1);
-        wz = __ldg(src.dirs + 3ull * i + 2);
-        wt = __ldg(src.weights + i);
-      } else {
-        const float4 c = src.geom[4ull * i + 2], d = src.geom[4ull * i + 3];
-        wx = c.y;
-        wy = c.z;
-        wz = c.w;
-        wt = d.x;
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 64; ++k) v[k] = 0.0f;
-    }
-    store_row_bf16(act, tid, v);
-    // forward
-    for (int l = 0; l < 5 && !failed; ++l) {
-      sync_for_mma();
-      const uint32_t N = l < 4 ? 64u : 48u;
-      if (tid == 0) issue_layer(tmem + TM_FWD, act + l * TILE, w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, N, &mbar);
-      wait_mma();
-      if (failed) break;
-      if (l < 4) {
-        tc::tmem_ld16x<4>(tmem + TM_FWD + lane_off, v);
-        store_row_bias_relu(act + (l + 1) * TILE, tid, v, s_b + 64 * l);
-      } else {
-        tc::tmem_ld16x<3>(tmem + TM_FWD + lane_off, v);
-      }
-      tc::fence_before_sync();
-    }
-    if (failed) break;
-    // loss gradient at the output (40 values, padded with zeros to 64)
-    float g[64];
-    {
-      float o[40];
-#pragma unroll
-      for (int k = 0; k < 40; ++k) o[k] = v[k] + s_b[4 * 64 + k];
-      float lsum = 0.0f;
-      if (valid && wt != 0.0f) {
-        const float il = rsqrtf(fmaxf(wx * wx + wy * wy + wz * wz, 1e-30f));
-        lsum = guide::loss_grad(o, wx * il, wy * il, wz * il, wt * inv_n, g);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 40; ++k) g[k] = 0.0f;
-      }
-#pragma unroll
-      for (int k = 40; k < 64; ++k) g[k] = 0.0f;
-#pragma unroll
-      for (int o2 = 16; o2 > 0; o2 >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o2);
-      if ((tid & 31) == 0) atomicAdd(&s_loss, lsum);
-    }
-    add_bias_grad(s_db + 4 * 64, g, 40);
-    // backward, layer 5 (index 4) down to layer 1 (index 0)
-    for (int l = 4; l >= 0 && !failed; --l) {
-      // dZ_l (registers g) -> tile l + 1: A of dH (K-major) and the upper
-      // 64-row block of A of dW (MN-major)
-      uint8_t* tl = act + l * TILE;
-      store_row_bf16(tl + TILE, tid, g);
-      sync_for_mma();
-      if (tid == 0) {
-        // dW_l += [H^T ; dZ^T] x (H^T)^T over the 128 samples (K = 128):
-        // both operands MN-major, 16 samples (two 8-row atoms) per step
-        const uint32_t idesc_mn = tc::idesc_bf16_f32_mn(128, 64);
-        const uint32_t sh = tc::smem_u32(tl);
-#pragma unroll
-        for (uint32_t ks = 0; ks < 8; ++ks) {
-          const uint32_t base = sh + ks * 2048;
-          tc::mma_bf16(tmem + TM_DW + 64 * l, tc::sw128_mn_desc(base, TILE), tc::sw128_mn_desc(base, TILE), idesc_mn,
-                       (first && ks == 0) ? 0u : 1u);
-        }
-        if (l > 0) {
-          // dH_{l-1} = dZ_l W_l  (B = W_l^T rows)
-          const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
-          const uint32_t sdz = sh + TILE, swt = tc::smem_u32(w + (R_T + 64 * (l - 1)) * 128);
-#pragma unroll
-          for (uint32_t k = 0; k < 4; ++k)
-            tc::mma_bf16(tmem + TM_DH, tc::sw128_desc(sdz + 32 * k), tc::sw128_desc(swt + 32 * k), idesc, k);
-        }
-        tc::mma_commit(&mbar);
-      }
-      wait_mma();
-      if (failed) break;
-      if (l > 0) {
-        // dZ_{l-1} = dH_{l-1} where H_{l-1} > 0: the BF16 bits of this
-        // sample's row of tile l, +-0 masked out
-        tc::tmem_ld16x<4>(tmem + TM_DH + lane_off, g);
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          const uint4 q = *(const uint4*)(tl + tid * 128 + ((c ^ (tid & 7)) << 4));
-          const uint32_t hw[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            if ((hw[j] & 0x7fffu) == 0u) g[8 * c + 2 * j] = 0.0f;
-            if ((hw[j] & 0x7fff0000u) == 0u) g[8 * c + 2 * j + 1] = 0.0f;
-          }
-        }
-        add_bias_grad(s_db + 64 * (l - 1), g, 64);
-      }
-      tc::fence_before_sync();
-    }
+    train_tile<SRC>(src, src.first + t * 128 + tid, n, inv_n, w, act, tmem, lane_off, &mbar, phase, first, &failed,
+                    status, s_b, s_db, &s_loss);
     first = false;
   }
-  // flush: dW (rows 64..127 of the accumulators) lives in the TMEM lanes of
-  // warps 2 and 3
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const bool ok = !failed && !first;
-  if (warp >= 2) {
-    const int o = (warp - 2) * 32 + (tid & 31);
-    for (int l = 0; l < 5; ++l) {
-      const int rows = l < 4 ? 64 : 40;
-      float d[64];
-      if (ok) {
+  flush_dw(tmem, lane_off, ok, [&](int l, int o, const float* d) {
+    float4* gw = reinterpret_cast<float4*>(slot + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) tc::tmem_ld16(tmem + TM_DW + 64 * l + lane_off + c * 16, d + c * 16);
-      } else {
-#pragma unroll
-        for (int c = 0; c < 64; ++c) d[c] = 0.0f;
-      }
-      if (o < rows) {
-        float4* gw = reinterpret_cast<float4*>(slot + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) gw[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
-      }
-    }
-  }
+    for (int k = 0; k < 16; ++k) gw[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
+  });
   __syncthreads();
   for (int k = tid; k < 4 * 64 + 40; k += 128) slot[P_B + k] = ok ? s_db[k] : 0.0f;
   if (tid == 0) loss_part[blockIdx.x] = ok ? s_loss : 0.0f;
-  if (tid == 0 && failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy: bounded second chance
+  if (tid == 0 && failed) {
+    tc::mbar_wait(&mbar_w, 0, 1u << 20);       // a late weight copy: bounded second chance
+    tc::mbar_wait(&mbar, phase ^ 1u, 1u << 20);  // and an MMA still in flight
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// All CTAs of a cooperative grid meet here: the k-th barrier of a launch
+// completes when the arrival counter (zeroed before the launch) reaches
+// (k + 1) x gridDim.x.  Memory written before the barrier (with a device
+// fence) is visible after it to loads that bypass L1.  The wait has an
+// iteration limit; false (the same in every thread of the CTA) when it
+// ran out, with the status bit set.
+__device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t k, uint32_t* status, volatile int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(counter, 1u);
+    const uint32_t target = (k + 1) * gridDim.x;
+    bool ok = false;
+    for (uint32_t it = 0; it < (1u << 22); ++it) {
+      uint32_t v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(counter) : "memory");
+      if (v >= target) {
+        ok = true;
+        break;
+      }
+      __nanosleep(64);
+    }
+    if (!ok) atomicOr(status, ST_GUIDE_NONFINITE << 1);
+    *s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// One wave's training rounds in one cooperative launch (one CTA per SM, all
+// resident): for each slice of `chunk` samples [s * chunk, (s + 1) * chunk)
+// of the batch (while the batch has samples), every CTA
+//   1. reads the current weights and biases (loads that bypass L1: other
+//      CTAs wrote them in the last round),
+//   2. runs its tiles of the slice (forward, loss gradient, backward),
+//   3. adds its dW, db and loss into acc (float atomics),
+// the grid meets, CTA c applies Adam to its share of the parameters (and
+// zeroes their sums for the next round), refreshing their FP32 master and
+// BF16 forward / transposed copies, and the grid meets again.  The same
+// steps as a training launch followed by an Adam launch per slice, without
+// their launches and per-launch set-up; the gradient sum's order differs
+// (atomics instead of per-CTA slots).  acc: NPARAM gradient sums, the loss
+// sum, then the barrier counter (word ACC_BAR), all zero at launch.
+constexpr int ACC_LOSS = NPARAM;
+constexpr int ACC_BAR = NPARAM + 32;
+constexpr int ACC_WORDS = NPARAM + 64;
+
+template <int SRC>
+__global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restrict__ pack, float* __restrict__ master,
+                                                               float* __restrict__ adam_m, float* __restrict__ adam_v,
+                                                               GuideSrc src, uint32_t chunk, uint32_t rounds,
+                                                               float lr, float* __restrict__ acc,
+                                                               float* __restrict__ loss_last, uint32_t* step_count,
+                                                               uint32_t* status,
+                                                               unsigned long long* __restrict__ sample_count) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = align1024(smem_raw);
+  uint8_t* w = smem;
+  uint8_t* act = smem + TRAIN_OFF_ACT;
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int failed;
+  __shared__ int bar_ok;
+  __shared__ float s_db[4 * 64 + 40];
+  __shared__ __align__(16) float s_b[4 * 64 + 48];
+  __shared__ float s_loss;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  uint32_t* counter = reinterpret_cast<uint32_t*>(acc + ACC_BAR);
+  const uint32_t n = src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n;
+  const uint32_t t0 = *(volatile const uint32_t*)step_count;  // Adam steps before this launch
+  if (tid == 0) {
+    tc::mbar_init(&mbar, 1);
+    tc::fence_mbar_init();
+    failed = 0;
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_base;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const float inv_n = 1.0f / (float)chunk;
+  // this CTA's share of the parameters for the Adam step
+  const uint32_t share = (NPARAM + gridDim.x - 1) / gridDim.x;
+  const uint32_t p0 = blockIdx.x * share, p1 = min(p0 + share, (uint32_t)NPARAM);
+  uint32_t phase = 0, bars = 0, done = 0;
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t first = r * chunk;
+    if (first >= n) break;  // the same in every CTA
+    const uint32_t last = min(first + chunk, n);
+    // 1. weights and biases of the last round
+    {
+      const uint4* g4 = reinterpret_cast<const uint4*>(pack);
+      uint4* s4 = reinterpret_cast<uint4*>(w);
+#pragma unroll 5
+      for (int k = tid; k < PACK_BYTES / 16; k += 128) s4[k] = __ldcg(g4 + k);
+      for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldcg(master + P_B + k) : 0.0f;
+      for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
+      if (tid == 0) s_loss = 0.0f;
+    }
+    tc::fence_smem_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // 2. this CTA's tiles of the slice
+    const uint32_t ntiles = (last - first + 127) / 128;
+    bool any = false;
+    for (uint32_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
+      train_tile<SRC>(src, first + t * 128 + tid, last, inv_n, w, act, tmem, lane_off, &mbar, phase, !any, &failed,
+                      status, s_b, s_db, &s_loss);
+      any = true;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // 3. sums into acc
+    if (any && !failed) {
+      flush_dw(tmem, lane_off, true, [&](int l, int o, const float* d) {
+        float4* gw = reinterpret_cast<float4*>(acc + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) atomicAdd(gw + k, make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]));
+      });
+      for (int k = tid; k < 4 * 64 + 40; k += 128) atomicAdd(acc + P_B + k, s_db[k]);
+      if (tid == 0) atomicAdd(acc + ACC_LOSS, s_loss);
+    }
+    if (!grid_barrier(counter, bars++, status, &bar_ok) || failed) break;
+    // Adam on this CTA's share (the step of k_guide_adam)
+    const float t = (float)(t0 + done + 1);
+    const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
+    for (uint32_t i = p0 + tid; i < p1; i += 128) {
+      const float gi = __ldcg(acc + i);
+      acc[i] = 0.0f;
+      if (!isfinite(gi)) {
+        atomicOr(status, ST_GUIDE_NONFINITE);
+        continue;
+      }
+      const float mi = 0.9f * __ldcg(adam_m + i) + 0.1f * gi;
+      const float vi = 0.999f * __ldcg(adam_v + i) + 0.001f * gi * gi;
+      adam_m[i] = mi;
+      adam_v[i] = vi;
+      const float wv = __ldcg(master + i) - lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
+      master[i] = wv;
+      if (i < P_W5) {
+        const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
+        pack_store(pack, R_FWD + l * 64 + o, k, wv);
+        if (l >= 1) pack_store(pack, R_T + (l - 1) * 64 + k, o, wv);
+      } else if (i < P_B) {
+        const int o = (i - P_W5) >> 6, k = (i - P_W5) & 63;
+        pack_store(pack, R_W5 + o, k, wv);
+        pack_store(pack, R_T + 3 * 64 + k, o, wv);
+      }
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+      *loss_last = __ldcg(acc + ACC_LOSS);
+      acc[ACC_LOSS] = 0.0f;
+    }
+    ++done;
+    if (!grid_barrier(counter, bars++, status, &bar_ok)) break;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    *step_count = t0 + done;
+    if (sample_count) *sample_count += min(n, done * chunk);
+  }
+  // after a time-out, an MMA may still be in flight (its completion has the
+  // parity before the last toggle): a bounded chance to finish before its
+  // TMEM is freed
+  if (tid == 0 && failed) tc::mbar_wait(&mbar, phase ^ 1u, 1u << 20);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -540,6 +734,34 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float 
   return Status();
 }
 
+// One wave's training rounds (k_guide_train_rounds), a cooperative launch
+// of one CTA per SM; acc (ACC_WORDS floats) is zeroed first.
+Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, uint32_t chunk, uint32_t rounds, float lr,
+                                 float* acc, cudaStream_t s, unsigned long long* sample_count) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    LISA_CUDA(cudaFuncSetAttribute(k_guide_train_rounds<SRC_GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TRAIN_SMEM));
+    attr_set = true;
+  }
+  LISA_CUDA(cudaMemsetAsync(acc, 0, sizeof(float) * ACC_WORDS, s));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)sm_count_current());
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = TRAIN_SMEM;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_GEOM>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
+                               chunk, rounds, lr, acc, g.loss_last, g.d_step, g.status, sample_count));
+  return Status();
+}
+
+size_t guide_train_acc_words() { return ACC_WORDS; }
+
 // g.grads and g.loss = the sums of the last training launch's partials.
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s) {
   k_guide_reduce<<<(NPARAM + 255) / 256, 256, 0, s>>>(g.grad_part, g.loss_part, g.nparts, g.grads, g.loss);
@@ -598,6 +820,7 @@ Status guide_renderer_init(Renderer& r) {
   if (r.opts.estimator == LISA_ESTIMATOR_PHYSICAL)
     LISA_TRY(r.arena.alloc((void**)&r.nee_light, sizeof(float4) * 2ull * r.capacity, "emitter samples"));
   LISA_TRY(r.arena.alloc((void**)&r.guide_batch, sizeof(float4) * 4ull * B, "guide batch"));
+  LISA_TRY(r.arena.alloc((void**)&r.guide_acc, sizeof(float) * guide_train_acc_words(), "guide gradient sums"));
   return Status();
 }
 

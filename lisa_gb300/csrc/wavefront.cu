@@ -1470,17 +1470,12 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
     if (guided && waves[wv].train) {
       const uint32_t steps = waves[wv].steps;
       LISA_TRY(stage(5, [&] { return guide_collect(r, (int)wv, steps * r.guide_chunk, r.stream); }));
-      // one Adam step per slice of the collected samples
-      for (uint32_t k = 0; k < steps; ++k) {
-        GuideSrc slice = train_src;
-        slice.first = k * r.guide_chunk;
-        slice.n = (k + 1) * r.guide_chunk;
-        LISA_TRY(stage(5, [&] {
-          return guide_launch_train(*net, slice, SRC_GEOM, 1.0f / (float)r.guide_chunk, r.guide_chunk, r.stream,
-                                    true, &r.ctrl->train_samples);
-        }));
-        LISA_TRY(stage(5, [&] { return guide_launch_adam(*net, r.opts.guide_lr, r.stream, slice.count, slice.first); }));
-      }
+      // one Adam step per slice of the collected samples, all in one
+      // cooperative launch
+      LISA_TRY(stage(5, [&] {
+        return guide_launch_train_rounds(*net, train_src, r.guide_chunk, steps, r.opts.guide_lr, r.guide_acc, r.stream,
+                                         &r.ctrl->train_samples);
+      }));
     }
   }
   if (st) {
