@@ -466,22 +466,23 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t k, uint
 //      CTAs wrote them in the last round),
 //   2. runs its tiles of the slice (forward, loss gradient, backward),
 //   3. adds its dW, db and loss into acc (float atomics),
-// the grid meets, CTA c applies Adam to its share of the parameters (and
-// zeroes their sums for the next round), refreshing their FP32 master and
-// BF16 forward / transposed copies, and the grid meets again.  The same
-// steps as a training launch followed by an Adam launch per slice, without
-// their launches and per-launch set-up; the gradient sum's order differs
-// (atomics instead of per-CTA slots).  acc: NPARAM gradient sums, the loss
-// sum, then the barrier counter (word ACC_BAR), all zero at launch.
-constexpr int ACC_LOSS = NPARAM;
-constexpr int ACC_BAR = NPARAM + 32;
-constexpr int ACC_WORDS = NPARAM + 64;
+//   3. writes its dW, db and loss to its own slot of part / loss_part,
+// the grid meets, CTA c sums the slots over its share of 128 parameters
+// (the same order as k_guide_adam: deterministic) and applies Adam to
+// them, refreshing their FP32 master and BF16 forward / transposed copies,
+// and the grid meets again.  The same steps as a training launch followed
+// by an Adam launch per slice, without their launches and per-launch
+// set-up.  acc: the grid barrier's counter (word ACC_BAR), zero at launch.
+constexpr int ACC_BAR = 0;
+constexpr int ACC_WORDS = 64;
+constexpr uint32_t ADAM_SHARE = 128;  // parameters per CTA in the Adam phase (a multiple of 4)
 
 template <int SRC>
 __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restrict__ pack, float* __restrict__ master,
                                                                float* __restrict__ adam_m, float* __restrict__ adam_v,
                                                                GuideSrc src, uint32_t chunk, uint32_t rounds,
-                                                               float lr, float* __restrict__ acc,
+                                                               float lr, float* __restrict__ part,
+                                                               float* __restrict__ loss_part, float* __restrict__ acc,
                                                                float* __restrict__ loss_last, uint32_t* step_count,
                                                                uint32_t* status,
                                                                unsigned long long* __restrict__ sample_count) {
@@ -490,6 +491,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
   uint8_t* w = smem;
   uint8_t* act = smem + TRAIN_OFF_ACT;
   __shared__ uint64_t mbar;
+  __shared__ uint64_t mbar_w;  // the weights' bulk copy, once per round
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   __shared__ int bar_ok;
@@ -502,6 +504,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
   const uint32_t t0 = *(volatile const uint32_t*)step_count;  // Adam steps before this launch
   if (tid == 0) {
     tc::mbar_init(&mbar, 1);
+    tc::mbar_init(&mbar_w, 1);
     tc::fence_mbar_init();
     failed = 0;
   }
@@ -512,23 +515,37 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
   const uint32_t tmem = tmem_base;
   const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
   const float inv_n = 1.0f / (float)chunk;
-  // this CTA's share of the parameters for the Adam step
-  const uint32_t share = (NPARAM + gridDim.x - 1) / gridDim.x;
-  const uint32_t p0 = blockIdx.x * share, p1 = min(p0 + share, (uint32_t)NPARAM);
-  uint32_t phase = 0, bars = 0, done = 0;
+  // the Adam phase: for each share of 128 parameters p0.. of this CTA,
+  // thread (g, q) = (tid / 4, tid % 4) sums the slots j = q (mod 4) of
+  // parameters p0 + 4 g .. + 3 (one float4 a slot); the quad's sums meet by
+  // shuffles and thread (g, q) updates parameter p0 + 4 g + q
+  const uint32_t qq = tid & 3;
+  float* slot = part + (size_t)blockIdx.x * NPARAM;
+  uint32_t phase = 0, wphase = 0, bars = 0, done = 0;
+  bool w_busy = false;  // thread 0: a weight copy not waited for
   for (uint32_t r = 0; r < rounds; ++r) {
     const uint32_t first = r * chunk;
     if (first >= n) break;  // the same in every CTA
     const uint32_t last = min(first + chunk, n);
-    // 1. weights and biases of the last round
-    {
-      const uint4* g4 = reinterpret_cast<const uint4*>(pack);
-      uint4* s4 = reinterpret_cast<uint4*>(w);
-#pragma unroll 5
-      for (int k = tid; k < PACK_BYTES / 16; k += 128) s4[k] = __ldcg(g4 + k);
-      for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldcg(master + P_B + k) : 0.0f;
-      for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
-      if (tid == 0) s_loss = 0.0f;
+    // 1. weights (bulk copy; the other CTAs' generic-proxy writes of the
+    // last round are ordered before it by the grid barrier and the proxy
+    // fence) and biases (loads that bypass L1)
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      tc::bulk_load(w, pack, PACK_BYTES, &mbar_w);
+      w_busy = true;
+    }
+    for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldcg(master + P_B + k) : 0.0f;
+    for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
+    if (tid == 0) {
+      s_loss = 0.0f;
+      if (tc::mbar_wait(&mbar_w, wphase)) {
+        w_busy = false;
+      } else {
+        atomicOr(status, ST_GUIDE_NONFINITE << 1);
+        failed = 1;
+      }
+      wphase ^= 1u;
     }
     tc::fence_smem_async();
     tc::fence_before_sync();
@@ -545,47 +562,70 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    // 3. sums into acc
-    if (any && !failed) {
-      flush_dw(tmem, lane_off, true, [&](int l, int o, const float* d) {
-        float4* gw = reinterpret_cast<float4*>(acc + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64);
+    // 3. this CTA's slot (zeros when it had no tile this round)
+    const bool ok = any && !failed;
+    flush_dw(tmem, lane_off, ok, [&](int l, int o, const float* d) {
+      float4* gw = reinterpret_cast<float4*>(slot + (l < 4 ? P_W + l * 4096 : P_W5) + o * 64);
 #pragma unroll
-        for (int k = 0; k < 16; ++k) atomicAdd(gw + k, make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]));
-      });
-      for (int k = tid; k < 4 * 64 + 40; k += 128) atomicAdd(acc + P_B + k, s_db[k]);
-      if (tid == 0) atomicAdd(acc + ACC_LOSS, s_loss);
-    }
+      for (int k = 0; k < 16; ++k) gw[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
+    });
+    for (int k = tid; k < 4 * 64 + 40; k += 128) slot[P_B + k] = ok ? s_db[k] : 0.0f;
+    if (tid == 0) loss_part[blockIdx.x] = ok ? s_loss : 0.0f;
     if (!grid_barrier(counter, bars++, status, &bar_ok) || failed) break;
     // Adam on this CTA's share (the step of k_guide_adam)
     const float t = (float)(t0 + done + 1);
     const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
-    for (uint32_t i = p0 + tid; i < p1; i += 128) {
-      const float gi = __ldcg(acc + i);
-      acc[i] = 0.0f;
-      if (!isfinite(gi)) {
-        atomicOr(status, ST_GUIDE_NONFINITE);
-        continue;
+    if (blockIdx.x == 0 && warp == 0) {
+      float l = 0.0f;
+      for (uint32_t j = tid; j < gridDim.x; j += 32) l += __ldcg(loss_part + j);
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) l += __shfl_xor_sync(0xffffffffu, l, m);
+      if (tid == 0) *loss_last = l;
+    }
+    for (uint32_t p0 = blockIdx.x * ADAM_SHARE; p0 < (uint32_t)NPARAM; p0 += gridDim.x * ADAM_SHARE) {
+      const uint32_t pq = p0 + 4u * (tid >> 2);
+      float4 g4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (pq < (uint32_t)NPARAM) {
+#pragma unroll 8
+        for (uint32_t j = qq; j < gridDim.x; j += 4) {
+          const float4 x = __ldcg(reinterpret_cast<const float4*>(part + (size_t)j * NPARAM + pq));
+          g4.x += x.x;
+          g4.y += x.y;
+          g4.z += x.z;
+          g4.w += x.w;
+        }
       }
-      const float mi = 0.9f * __ldcg(adam_m + i) + 0.1f * gi;
-      const float vi = 0.999f * __ldcg(adam_v + i) + 0.001f * gi * gi;
-      adam_m[i] = mi;
-      adam_v[i] = vi;
-      const float wv = __ldcg(master + i) - lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
-      master[i] = wv;
-      if (i < P_W5) {
-        const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
-        pack_store(pack, R_FWD + l * 64 + o, k, wv);
-        if (l >= 1) pack_store(pack, R_T + (l - 1) * 64 + k, o, wv);
-      } else if (i < P_B) {
-        const int o = (i - P_W5) >> 6, k = (i - P_W5) & 63;
-        pack_store(pack, R_W5 + o, k, wv);
-        pack_store(pack, R_T + 3 * 64 + k, o, wv);
+#pragma unroll
+      for (int m = 1; m <= 2; m <<= 1) {
+        g4.x += __shfl_xor_sync(0xffffffffu, g4.x, m);
+        g4.y += __shfl_xor_sync(0xffffffffu, g4.y, m);
+        g4.z += __shfl_xor_sync(0xffffffffu, g4.z, m);
+        g4.w += __shfl_xor_sync(0xffffffffu, g4.w, m);
+      }
+      const uint32_t i = pq + qq;
+      const float gi = qq == 0 ? g4.x : qq == 1 ? g4.y : qq == 2 ? g4.z : g4.w;
+      if (i < (uint32_t)NPARAM) {
+        if (!isfinite(gi)) atomicOr(status, ST_GUIDE_NONFINITE);
+        else {
+          const float mi = 0.9f * __ldcg(adam_m + i) + 0.1f * gi;
+          const float vi = 0.999f * __ldcg(adam_v + i) + 0.001f * gi * gi;
+          adam_m[i] = mi;
+          adam_v[i] = vi;
+          const float wv = __ldcg(master + i) - lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
+          master[i] = wv;
+          if (i < P_W5) {
+            const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
+            pack_store(pack, R_FWD + l * 64 + o, k, wv);
+            if (l >= 1) pack_store(pack, R_T + (l - 1) * 64 + k, o, wv);
+          } else if (i < P_B) {
+            const int o = (i - P_W5) >> 6, k = (i - P_W5) & 63;
+            pack_store(pack, R_W5 + o, k, wv);
+            pack_store(pack, R_T + 3 * 64 + k, o, wv);
+          }
+        }
       }
     }
-    if (blockIdx.x == 0 && tid == 0) {
-      *loss_last = __ldcg(acc + ACC_LOSS);
-      acc[ACC_LOSS] = 0.0f;
-    }
+    asm volatile("fence.proxy.async.global;" ::: "memory");  // the pack, read next round by bulk copies
     ++done;
     if (!grid_barrier(counter, bars++, status, &bar_ok)) break;
   }
@@ -597,6 +637,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
   // parity before the last toggle): a bounded chance to finish before its
   // TMEM is freed
   if (tid == 0 && failed) tc::mbar_wait(&mbar, phase ^ 1u, 1u << 20);
+  if (tid == 0 && w_busy) tc::mbar_wait(&mbar_w, wphase ^ 1u, 1u << 20);  // a late weight copy
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -755,8 +796,10 @@ Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, uint32_t chun
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (!g.grad_part) return Status::invalid("guide: no partial-gradient slots");  // one per SM
   LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_GEOM>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
-                               chunk, rounds, lr, acc, g.loss_last, g.d_step, g.status, sample_count));
+                               chunk, rounds, lr, g.grad_part, g.loss_part, acc, g.loss_last, g.d_step, g.status,
+                               sample_count));
   return Status();
 }
 
