@@ -162,7 +162,8 @@ def mlp_roofline(guided_row):
     """Tensor-pipe roofline of the guide's kernels inside the guided render:
     inference (k_guided_infer: the network on every emitter-queue entry of a
     guided depth, fused with the guided bounce) and training (sample
-    collection, k_guide_train, Adam), from the renderer's stage timers and
+    collection, then k_guide_train_rounds: every Adam round of a wave in one
+    cooperative launch), from the renderer's stage timers and
     its work counters, against the sustained bf16 peak (the kernels run
     inside a long render)."""
     peak, kind = measured_peak_bf16(sustained=True)
