@@ -370,6 +370,14 @@ int lisa_guide_forward(lisa_guide* g, const float* features, uint32_t n, float* 
 int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dirs,
                           const float* weights, uint32_t n, float lr, float* loss,
                           float* grads);
+/* Up to `steps` training steps with Adam (learning rate lr > 0), step k on
+ * samples [k * chunk, (k + 1) * chunk) of the n given (chunk a multiple of
+ * 128; the steps end with the samples), all in one launch: the same
+ * updates, bit for bit, as lisa_guide_train_step on each slice in turn.
+ * Writes the last step's loss. */
+int lisa_guide_train_steps(lisa_guide* g, const float* features, const float* dirs,
+                           const float* weights, uint32_t n, uint32_t chunk, uint32_t steps,
+                           float lr, float* loss);
 /* The guide a renderer trains in guided mode (borrowed). */
 int lisa_renderer_guide(lisa_renderer* r, int32_t scene, lisa_guide** out);
 

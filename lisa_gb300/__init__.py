@@ -282,6 +282,17 @@ class Guide:
                                               C.cast(C.byref(loss), C.c_void_p), _ptr(g)))
         return float(loss.value), g
 
+    def train_steps(self, features, dirs, weights, chunk: int, steps: int, lr: float) -> float:
+        """Adam steps on consecutive slices of `chunk` samples, in one launch
+        (the same updates as train_step on each slice); the last step's loss."""
+        x = np.ascontiguousarray(np.asarray(features, np.float32).reshape(-1, N.GUIDE_IN))
+        d = np.ascontiguousarray(np.asarray(dirs, np.float32).reshape(-1, 3))
+        w = np.ascontiguousarray(np.asarray(weights, np.float32).reshape(-1))
+        loss = C.c_float()
+        N.check(N.lib().lisa_guide_train_steps(self._h, _ptr(x), _ptr(d), _ptr(w), x.shape[0], int(chunk), int(steps),
+                                               float(lr), C.cast(C.byref(loss), C.c_void_p)))
+        return float(loss.value)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h and getattr(self, "_own", False):

@@ -58,6 +58,17 @@ __global__ void k_guide_pack(const float* __restrict__ master, uint16_t* __restr
 }
 
 
+// One Adam update (Kingma & Ba 2015; beta1 0.9, beta2 0.999, eps 1e-8) of
+// weight w with gradient g; m, v in/out.  Written with explicitly rounded
+// operations (no contraction), so the separate Adam kernel and the training
+// rounds give the same bits.
+__device__ __forceinline__ float adam_update(float w, float g, float& m, float& v, float lr, float b1c, float b2c) {
+  m = __fadd_rn(__fmul_rn(0.9f, m), __fmul_rn(0.1f, g));
+  v = __fadd_rn(__fmul_rn(0.999f, v), __fmul_rn(__fmul_rn(0.001f, g), g));
+  const float step = __fdiv_rn(__fmul_rn(lr, __fdiv_rn(m, b1c)), __fadd_rn(__fsqrt_rn(__fdiv_rn(v, b2c)), 1e-8f));
+  return __fsub_rn(w, step);
+}
+
 __device__ __forceinline__ void pack_store(uint16_t* pack, int row, int col, float v) {
   uint8_t* base = (uint8_t*)pack + (size_t)(row & ~7) * 128;
   *(uint16_t*)(base + tc::sw128_offset(row & 7, col)) = f2bf(v);
@@ -101,11 +112,10 @@ __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, 
     atomicOr(status, ST_GUIDE_NONFINITE);
     return;
   }
-  const float mi = 0.9f * m[i] + 0.1f * gi;
-  const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+  float mi = m[i], vi = v[i];
+  const float w = adam_update(master[i], gi, mi, vi, lr, b1c, b2c);
   m[i] = mi;
   v[i] = vi;
-  const float w = master[i] - lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
   master[i] = w;
   if (i < P_W5) {  // W1..W4 (output o, input k): forward row l*64+o; transposed for l >= 1
     const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
@@ -178,9 +188,11 @@ __device__ __forceinline__ void reduce_scatter_round(const float* in, float* out
   }
 }
 
-// Column sums of the warp's 32 rows of v[64] added to s_db[0 .. count):
-// a reduce-scatter by recursive halving leaves each lane two of the 64
-// column sums, which it adds with shared-memory atomics.
+// Column sums of the warp's 32 rows of v[64] added to the warp's own
+// s_db[0 .. count): a reduce-scatter by recursive halving leaves each lane
+// two of the 64 column sums (different columns in different lanes), which
+// it adds with plain stores -- no atomics, so the sums are the same in
+// every run.
 __device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int count) {
   float a[32], b[16], c[8], d[4], e[2];
   reduce_scatter_round<64>(v, a, 16);
@@ -191,13 +203,23 @@ __device__ __forceinline__ void add_bias_grad(float* s_db, const float* v, int c
   const int lane = threadIdx.x & 31;
   const int col = ((lane & 16) ? 32 : 0) + ((lane & 8) ? 16 : 0) + ((lane & 4) ? 8 : 0) + ((lane & 2) ? 4 : 0) +
                   ((lane & 1) ? 2 : 0);
-  if (col < count) atomicAdd(&s_db[col], e[0]);
-  if (col + 1 < count) atomicAdd(&s_db[col + 1], e[1]);
+  if (col < count) s_db[col] += e[0];
+  if (col + 1 < count) s_db[col + 1] += e[1];
+}
+
+constexpr int DB_WORDS = 4 * 64 + 40;  // bias gradients of the five layers
+
+// Bias gradient k (or, for k == DB_WORDS, the loss) of the CTA: the four
+// warps' sums in warp order.
+__device__ __forceinline__ float bias_grad_total(const float* s_db, const float* s_loss, int k) {
+  if (k == DB_WORDS) return ((s_loss[0] + s_loss[1]) + s_loss[2]) + s_loss[3];
+  return ((s_db[k] + s_db[DB_WORDS + k]) + s_db[2 * DB_WORDS + k]) + s_db[3 * DB_WORDS + k];
 }
 
 // Forward, loss gradient and backward of one 128-sample tile (thread t owns
 // sample i = row t): dW accumulates in TMEM (initialised by the first tile
-// of a batch), db and the loss in shared memory.  The caller has the weights
+// of a batch), db and the loss in per-warp shared-memory sums (s_db: 4 x
+// DB_WORDS, s_loss: 4), added up in warp order by bias_grad_total.  The caller has the weights
 // (w) and biases (s_b) in shared memory and has met at a barrier since.
 template <int SRC>
 __device__ __forceinline__ void train_tile(const GuideSrc& src, uint32_t i, uint32_t n, float inv_n, uint8_t* w,
@@ -275,9 +297,10 @@ __device__ __forceinline__ void train_tile(const GuideSrc& src, uint32_t i, uint
     for (int k = 40; k < 64; ++k) g[k] = 0.0f;
 #pragma unroll
     for (int o2 = 16; o2 > 0; o2 >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o2);
-    if ((tid & 31) == 0) atomicAdd(s_loss, lsum);
+    if ((tid & 31) == 0) s_loss[tid >> 5] += lsum;
   }
-  add_bias_grad(s_db + 4 * 64, g, 40);
+  float* const s_dbw = s_db + (tid >> 5) * DB_WORDS;  // this warp's sums
+  add_bias_grad(s_dbw + 4 * 64, g, 40);
   // backward, layer 5 (index 4) down to layer 1 (index 0)
   for (int l = 4; l >= 0; --l) {
     // dZ_l (registers g) -> tile l + 1: A of dH (K-major) and the upper
@@ -322,7 +345,7 @@ __device__ __forceinline__ void train_tile(const GuideSrc& src, uint32_t i, uint
           if ((hw[j] & 0x7fff0000u) == 0u) g[8 * c + 2 * j + 1] = 0.0f;
         }
       }
-      add_bias_grad(s_db + 64 * (l - 1), g, 64);
+      add_bias_grad(s_dbw + 64 * (l - 1), g, 64);
     }
     tc::fence_before_sync();
   }
@@ -364,9 +387,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   __shared__ uint64_t mbar_w;  // the packed weights' bulk copy
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
-  __shared__ float s_db[4 * 64 + 40];
+  __shared__ float s_db[4 * DB_WORDS];  // per warp
   __shared__ __align__(16) float s_b[4 * 64 + 48];  // biases
-  __shared__ float s_loss;
+  __shared__ float s_loss[4];
   const int tid = threadIdx.x, warp = tid >> 5;
   // samples [src.first, n)
   const uint32_t n = max(src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n, src.first);
@@ -386,9 +409,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
     tc::fence_mbar_init();
     tc::bulk_load(w, pack, PACK_BYTES, &mbar_w);  // weights by TMA while the rest is set up
     failed = 0;
-    s_loss = 0.0f;
   }
-  for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
+  if (tid < 4) s_loss[tid] = 0.0f;
+  for (int k = tid; k < 4 * DB_WORDS; k += 128) s_db[k] = 0.0f;
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldg(master + P_B + k) : 0.0f;
   if (tid == 0 && !tc::mbar_wait(&mbar_w, 0)) {
@@ -405,7 +428,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   bool first = true;
   for (uint32_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
     train_tile<SRC>(src, src.first + t * 128 + tid, n, inv_n, w, act, tmem, lane_off, &mbar, phase, first, &failed,
-                    status, s_b, s_db, &s_loss);
+                    status, s_b, s_db, s_loss);
     first = false;
   }
   tc::fence_before_sync();
@@ -418,8 +441,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
     for (int k = 0; k < 16; ++k) gw[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
   });
   __syncthreads();
-  for (int k = tid; k < 4 * 64 + 40; k += 128) slot[P_B + k] = ok ? s_db[k] : 0.0f;
-  if (tid == 0) loss_part[blockIdx.x] = ok ? s_loss : 0.0f;
+  for (int k = tid; k < DB_WORDS; k += 128) slot[P_B + k] = ok ? bias_grad_total(s_db, s_loss, k) : 0.0f;
+  if (tid == 0) loss_part[blockIdx.x] = ok ? bias_grad_total(s_db, s_loss, DB_WORDS) : 0.0f;
   if (tid == 0 && failed) {
     tc::mbar_wait(&mbar_w, 0, 1u << 20);       // a late weight copy: bounded second chance
     tc::mbar_wait(&mbar, phase ^ 1u, 1u << 20);  // and an MMA still in flight
@@ -495,9 +518,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   __shared__ int bar_ok;
-  __shared__ float s_db[4 * 64 + 40];
+  __shared__ float s_db[4 * DB_WORDS];  // per warp
   __shared__ __align__(16) float s_b[4 * 64 + 48];
-  __shared__ float s_loss;
+  __shared__ float s_loss[4];
   const int tid = threadIdx.x, warp = tid >> 5;
   uint32_t* counter = reinterpret_cast<uint32_t*>(acc + ACC_BAR);
   const uint32_t n = src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n;
@@ -536,9 +559,9 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
       w_busy = true;
     }
     for (int k = tid; k < 4 * 64 + 48; k += 128) s_b[k] = k < 4 * 64 + 40 ? __ldcg(master + P_B + k) : 0.0f;
-    for (int k = tid; k < 4 * 64 + 40; k += 128) s_db[k] = 0.0f;
+    for (int k = tid; k < 4 * DB_WORDS; k += 128) s_db[k] = 0.0f;
+    if (tid < 4) s_loss[tid] = 0.0f;
     if (tid == 0) {
-      s_loss = 0.0f;
       if (tc::mbar_wait(&mbar_w, wphase)) {
         w_busy = false;
       } else {
@@ -556,7 +579,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
     bool any = false;
     for (uint32_t t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
       train_tile<SRC>(src, first + t * 128 + tid, last, inv_n, w, act, tmem, lane_off, &mbar, phase, !any, &failed,
-                      status, s_b, s_db, &s_loss);
+                      status, s_b, s_db, s_loss);
       any = true;
     }
     tc::fence_before_sync();
@@ -569,8 +592,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
 #pragma unroll
       for (int k = 0; k < 16; ++k) gw[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
     });
-    for (int k = tid; k < 4 * 64 + 40; k += 128) slot[P_B + k] = ok ? s_db[k] : 0.0f;
-    if (tid == 0) loss_part[blockIdx.x] = ok ? s_loss : 0.0f;
+    for (int k = tid; k < DB_WORDS; k += 128) slot[P_B + k] = ok ? bias_grad_total(s_db, s_loss, k) : 0.0f;
+    if (tid == 0) loss_part[blockIdx.x] = ok ? bias_grad_total(s_db, s_loss, DB_WORDS) : 0.0f;
     if (!grid_barrier(counter, bars++, status, &bar_ok) || failed) break;
     // Adam on this CTA's share (the step of k_guide_adam)
     const float t = (float)(t0 + done + 1);
@@ -607,11 +630,10 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
       if (i < (uint32_t)NPARAM) {
         if (!isfinite(gi)) atomicOr(status, ST_GUIDE_NONFINITE);
         else {
-          const float mi = 0.9f * __ldcg(adam_m + i) + 0.1f * gi;
-          const float vi = 0.999f * __ldcg(adam_v + i) + 0.001f * gi * gi;
+          float mi = __ldcg(adam_m + i), vi = __ldcg(adam_v + i);
+          const float wv = adam_update(__ldcg(master + i), gi, mi, vi, lr, b1c, b2c);
           adam_m[i] = mi;
           adam_v[i] = vi;
-          const float wv = __ldcg(master + i) - lr * (mi / b1c) / (sqrtf(vi / b2c) + 1e-8f);
           master[i] = wv;
           if (i < P_W5) {
             const int l = i >> 12, o = (i >> 6) & 63, k = i & 63;
@@ -777,11 +799,13 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float 
 
 // One wave's training rounds (k_guide_train_rounds), a cooperative launch
 // of one CTA per SM; acc (ACC_WORDS floats) is zeroed first.
-Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, uint32_t chunk, uint32_t rounds, float lr,
-                                 float* acc, cudaStream_t s, unsigned long long* sample_count) {
+Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, int src_kind, uint32_t chunk, uint32_t rounds,
+                                 float lr, float* acc, cudaStream_t s, unsigned long long* sample_count) {
   static bool attr_set = false;
   if (!attr_set) {
     LISA_CUDA(cudaFuncSetAttribute(k_guide_train_rounds<SRC_GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TRAIN_SMEM));
+    LISA_CUDA(cudaFuncSetAttribute(k_guide_train_rounds<SRC_RAW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    TRAIN_SMEM));
     attr_set = true;
   }
@@ -797,9 +821,14 @@ Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, uint32_t chun
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (!g.grad_part) return Status::invalid("guide: no partial-gradient slots");  // one per SM
-  LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_GEOM>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
-                               chunk, rounds, lr, g.grad_part, g.loss_part, acc, g.loss_last, g.d_step, g.status,
-                               sample_count));
+  if (src_kind == SRC_RAW)
+    LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_RAW>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
+                                 chunk, rounds, lr, g.grad_part, g.loss_part, acc, g.loss_last, g.d_step, g.status,
+                                 sample_count));
+  else
+    LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_GEOM>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
+                                 chunk, rounds, lr, g.grad_part, g.loss_part, acc, g.loss_last, g.d_step, g.status,
+                                 sample_count));
   return Status();
 }
 
@@ -1018,5 +1047,38 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
   return gret(s);
 }
 
+int lisa_guide_train_steps(lisa_guide* g, const float* features, const float* dirs, const float* weights, uint32_t n,
+                           uint32_t chunk, uint32_t steps, float lr, float* loss) {
+  if (!g || !features || !dirs || !weights) return gret(Status::invalid("null argument"));
+  if (n == 0 || steps == 0) return gret(Status::invalid("empty batch"));
+  if (chunk == 0 || chunk % 128) return gret(Status::invalid("chunk must be a positive multiple of 128"));
+  if (!(lr > 0.0f)) return gret(Status::invalid("lr must be positive"));
+  float *d_x = nullptr, *d_d = nullptr, *d_w = nullptr, *d_acc = nullptr;
+  auto run = [&]() -> Status {
+    LISA_CUDA(cudaMalloc(&d_x, sizeof(float) * 64ull * n));
+    LISA_CUDA(cudaMalloc(&d_d, sizeof(float) * 3ull * n));
+    LISA_CUDA(cudaMalloc(&d_w, sizeof(float) * n));
+    LISA_CUDA(cudaMalloc(&d_acc, sizeof(float) * guide_train_acc_words()));
+    LISA_CUDA(cudaMemcpyAsync(d_x, features, sizeof(float) * 64ull * n, cudaMemcpyHostToDevice, g->stream));
+    LISA_CUDA(cudaMemcpyAsync(d_d, dirs, sizeof(float) * 3ull * n, cudaMemcpyHostToDevice, g->stream));
+    LISA_CUDA(cudaMemcpyAsync(d_w, weights, sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
+    GuideSrc src;
+    std::memset(&src, 0, sizeof(src));
+    src.raw = d_x;
+    src.dirs = d_d;
+    src.weights = d_w;
+    src.n = n;
+    LISA_TRY(guide_launch_train_rounds(g->get(), src, SRC_RAW, chunk, steps, lr, d_acc, g->stream, nullptr));
+    if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->get().loss_last, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+    LISA_TRY(guide_check_status(g->get(), g->stream));
+    return Status();
+  };
+  Status s = run();
+  if (d_x) cudaFree(d_x);
+  if (d_d) cudaFree(d_d);
+  if (d_w) cudaFree(d_w);
+  if (d_acc) cudaFree(d_acc);
+  return gret(s);
+}
 
 }  // extern "C"

@@ -70,11 +70,11 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
 // step; sample_count (optional) accumulates the samples trained on
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
                           cudaStream_t s, bool adam_follows, unsigned long long* sample_count = nullptr);
-// A wave's training: up to `rounds` Adam steps on slices of `chunk` samples
-// of src (GEOM records), in one cooperative launch; acc is scratch of
+// Up to `rounds` Adam steps on slices of `chunk` samples of src (RAW or
+// GEOM), in one cooperative launch; acc is scratch of
 // guide_train_acc_words() floats
-Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, uint32_t chunk, uint32_t rounds, float lr,
-                                 float* acc, cudaStream_t s, unsigned long long* sample_count);
+Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, int src_kind, uint32_t chunk, uint32_t rounds,
+                                 float lr, float* acc, cudaStream_t s, unsigned long long* sample_count);
 size_t guide_train_acc_words();
 // g.grads / g.loss = sums of the last training launch's partials
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s);

@@ -77,6 +77,28 @@ def test_adam_update(gpu):
     np.testing.assert_allclose(after, ref, rtol=1e-5, atol=1e-6)
 
 
+def test_train_steps_equal_step_by_step_training(gpu):
+    """Several Adam steps in one cooperative launch (the renderer's training
+    path) against one train_step launch pair per slice: every CTA's
+    gradient goes to its own slot and the slots are summed in the same
+    order, so the parameters agree bit for bit.  Three slices of 1,024
+    samples with eight steps asked for: the steps end with the samples."""
+    p = _params(8)
+    X, d, w = _batch(3 * 1024, 9)
+    a = L.Guide(seed=1)
+    a.set_params(p)
+    loss_a = a.train_steps(X, d, w, chunk=1024, steps=8, lr=1e-2)
+    b = L.Guide(seed=1)
+    b.set_params(p)
+    for k in range(3):
+        sl = slice(1024 * k, 1024 * (k + 1))
+        loss_b, _ = b.train_step(X[sl], d[sl], w[sl], lr=1e-2, want_grads=False)
+    assert not np.array_equal(a.params(), p)
+    assert np.array_equal(a.params(), b.params())
+    # the loss of the last step (summed in another order)
+    assert abs(loss_a - loss_b) <= 1e-5 * abs(loss_b) + 1e-6, (loss_a, loss_b)
+
+
 def test_training_learns_a_direction_distribution(gpu):
     """Samples whose direction depends on the features: training with the
     kernels' own gradients raises the likelihood of held-out samples."""
