@@ -195,6 +195,13 @@ const char* lisa_version(void);
 /* SM count and compute capability of the current CUDA device.  Replaces the
  * device bring-up of OptixWrapper::init_optix (optix_wrapper.cc:39-52). */
 int lisa_device_info(int* sm_count, int* cc_major, int* cc_minor);
+/* Device memory that destroyed renderers left for reuse: renderers and BVH
+ * builds take their buffers from a per-process cache (at most
+ * LISA_DEVICE_CACHE_MB MiB of free blocks, default 8192; 0 turns it off),
+ * so a create-render-destroy cycle does not pay cudaMalloc/cudaFree each
+ * time.  This returns every cached block to the device and the number of
+ * bytes freed in *bytes (may be NULL). */
+int lisa_device_cache_release(uint64_t* bytes);
 
 /* ---- scene front end (host) ------------------------------------------- */
 

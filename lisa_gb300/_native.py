@@ -114,6 +114,7 @@ SIGNATURES = {
     "lisa_last_error": (C.c_char_p, []),
     "lisa_version": (C.c_char_p, []),
     "lisa_device_info": (C.c_int, [C.POINTER(C.c_int)] * 3),
+    "lisa_device_cache_release": (C.c_int, [C.POINTER(C.c_uint64)]),
     "lisa_scene_parse": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "lisa_scene_parse_string": (C.c_int, [C.c_char_p, C.c_size_t, C.c_char_p, C.POINTER(_P)]),
     "lisa_scene_params": (C.c_int, [_P, C.POINTER(RendererParams)]),

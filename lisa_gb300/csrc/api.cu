@@ -8,9 +8,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "guide.cuh"
@@ -42,13 +46,103 @@ static int ret(const Status& s) {
     return ret(Status(LISA_ERR_INVALID, "unknown error"));  \
   }
 
+// ---- device memory cache -----------------------------------------------------
+// Blocks are rounded up to 64 KiB (2 MiB above 32 MiB); a request takes the
+// smallest cached block of its device that is at least as large and at most
+// 1/8 + 2 MiB larger.  The cache holds at most LISA_DEVICE_CACHE_MB (default
+// 8192; 0 turns it off) of free blocks per process.  The state is never
+// destroyed (no CUDA call from a static destructor at process exit).
+namespace {
+struct DevCache {
+  std::mutex mu;
+  std::unordered_map<void*, std::pair<size_t, int>> live;  // block -> (rounded size, device)
+  std::multimap<std::pair<int, size_t>, void*> free_blocks;
+  size_t free_bytes = 0;
+  size_t cap = 0;
+  DevCache() {
+    const char* v = std::getenv("LISA_DEVICE_CACHE_MB");
+    cap = (size_t)(v ? std::strtoull(v, nullptr, 10) : 8192ull) << 20;
+  }
+  void release_locked() {
+    for (auto& kv : free_blocks) cudaFree(kv.second);
+    free_blocks.clear();
+    free_bytes = 0;
+  }
+};
+DevCache& dev_cache() {
+  static DevCache* c = new DevCache();
+  return *c;
+}
+size_t dev_round(size_t bytes) {
+  bytes = std::max<size_t>(bytes, 16);
+  const size_t g = bytes > (32ull << 20) ? (2ull << 20) : (64ull << 10);
+  return (bytes + g - 1) / g * g;
+}
+}  // namespace
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  DevCache& c = dev_cache();
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const size_t need = dev_round(bytes);
+  std::lock_guard<std::mutex> lock(c.mu);
+  auto it = c.free_blocks.lower_bound({dev, need});
+  if (it != c.free_blocks.end() && it->first.first == dev && it->first.second <= need + need / 8 + (2ull << 20)) {
+    *p = it->second;
+    c.live[it->second] = {it->first.second, dev};
+    c.free_bytes -= it->first.second;
+    c.free_blocks.erase(it);
+    return cudaSuccess;
+  }
+  void* q = nullptr;
+  e = cudaMalloc(&q, need);
+  if (e == cudaErrorMemoryAllocation && !c.free_blocks.empty()) {
+    cudaGetLastError();
+    c.release_locked();
+    e = cudaMalloc(&q, need);
+  }
+  if (e != cudaSuccess) return e;
+  c.live[q] = {need, dev};
+  *p = q;
+  return cudaSuccess;
+}
+
+void dev_free(void* p) {
+  if (!p) return;
+  DevCache& c = dev_cache();
+  std::lock_guard<std::mutex> lock(c.mu);
+  auto it = c.live.find(p);
+  if (it == c.live.end()) {  // not ours
+    cudaFree(p);
+    return;
+  }
+  const size_t bytes = it->second.first;
+  const int dev = it->second.second;
+  c.live.erase(it);
+  if (c.free_bytes + bytes <= c.cap) {
+    c.free_blocks.insert({{dev, bytes}, p});
+    c.free_bytes += bytes;
+  } else {
+    cudaFree(p);
+  }
+}
+
+size_t dev_cache_release() {
+  DevCache& c = dev_cache();
+  std::lock_guard<std::mutex> lock(c.mu);
+  const size_t n = c.free_bytes;
+  c.release_locked();
+  return n;
+}
+
 // ---- arena -----------------------------------------------------------------
 Status DeviceArena::alloc(void** p, size_t bytes, const char* what) {
   bytes = std::max<size_t>(bytes, 16);
   if (cap && used + bytes > cap)
     return Status(LISA_ERR_OOM, std::string("allocation cap exceeded by ") + what);
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, bytes);
+  cudaError_t e = dev_alloc(&q, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return Status(LISA_ERR_OOM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
@@ -60,14 +154,14 @@ Status DeviceArena::alloc(void** p, size_t bytes, const char* what) {
 }
 
 void DeviceArena::release_all() {
-  for (void* p : blocks) cudaFree(p);
+  for (void* p : blocks) dev_free(p);
   blocks.clear();
   used = 0;
 }
 
 Status TempDeviceBufs::get(void** p, size_t bytes, const char* what) {
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, std::max<size_t>(bytes, 16));
+  cudaError_t e = dev_alloc(&q, std::max<size_t>(bytes, 16));
   if (e != cudaSuccess) {
     cudaGetLastError();
     return Status(LISA_ERR_OOM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
@@ -78,7 +172,13 @@ Status TempDeviceBufs::get(void** p, size_t bytes, const char* what) {
 }
 
 TempDeviceBufs::~TempDeviceBufs() {
-  for (void* p : ptrs) cudaFree(p);
+  // the blocks go back to the cache, so the work that used them must be
+  // done (cudaFree used to wait for the device implicitly)
+  if (!ptrs.empty()) {
+    if (stream) cudaStreamSynchronize(stream);
+    else cudaDeviceSynchronize();
+  }
+  for (void* p : ptrs) dev_free(p);
 }
 
 Status BumpScratch::get(void** p, size_t bytes, const char* what) {
@@ -275,9 +375,9 @@ Status build_emitter_bvh(Renderer& r, const lisa_renderer_params& p, SceneGpu& s
   if (ne < EMIT_BVH_MIN_TRIS) return Status();  // the emitter search would not use it
   float* d_ev = nullptr;
   int32_t *d_gid = nullptr, *d_emat = nullptr;
-  cudaError_t e = cudaMalloc(&d_ev, sizeof(float) * ev.size());
-  if (e == cudaSuccess) e = cudaMalloc(&d_gid, sizeof(int32_t) * ne);
-  if (e == cudaSuccess) e = cudaMalloc(&d_emat, sizeof(int32_t) * ne);
+  cudaError_t e = dev_alloc((void**)&d_ev, sizeof(float) * ev.size());
+  if (e == cudaSuccess) e = dev_alloc((void**)&d_gid, sizeof(int32_t) * ne);
+  if (e == cudaSuccess) e = dev_alloc((void**)&d_emat, sizeof(int32_t) * ne);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_ev, ev.data(), sizeof(float) * ev.size(), cudaMemcpyHostToDevice, r.stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_gid, gid.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice, r.stream);
   if (e == cudaSuccess)
@@ -285,6 +385,7 @@ Status build_emitter_bvh(Renderer& r, const lisa_renderer_params& p, SceneGpu& s
   Status st = e == cudaSuccess ? Status() : Status::cuda(e, "emitter BVH upload");
   if (st.ok()) {
     TempDeviceBufs tmp;
+    tmp.stream = r.stream;
     st = build_bvh(d_ev, ne, r.stream, tmp, r.arena, &s.enodes, &s.etris, &s.ebvh, d_emat, r.opts.bvh_lbvh_only == 0);
     if (st.ok()) {
       k_emit_global_ids<<<r.sm_count * 4, 256, 0, r.stream>>>(s.etris, ne, d_gid);
@@ -293,9 +394,10 @@ Status build_emitter_bvh(Renderer& r, const lisa_renderer_params& p, SceneGpu& s
       if (e != cudaSuccess) st = Status::cuda(e, "emitter BVH indices");
     }
   }
-  if (d_ev) cudaFree(d_ev);
-  if (d_gid) cudaFree(d_gid);
-  if (d_emat) cudaFree(d_emat);
+  cudaStreamSynchronize(r.stream);  // before the blocks are reused
+  dev_free(d_ev);
+  dev_free(d_gid);
+  dev_free(d_emat);
   return st;
 }
 
@@ -315,9 +417,9 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
   float *d_v = nullptr, *d_n = nullptr;
   int32_t* d_m = nullptr;
   if (T) {
-    LISA_CUDA(cudaMalloc(&d_v, sizeof(float) * 9ull * T));
-    LISA_CUDA(cudaMalloc(&d_n, sizeof(float) * 9ull * T));
-    LISA_CUDA(cudaMalloc(&d_m, sizeof(int32_t) * T));
+    LISA_CUDA(dev_alloc((void**)&d_v, sizeof(float) * 9ull * T));
+    LISA_CUDA(dev_alloc((void**)&d_n, sizeof(float) * 9ull * T));
+    LISA_CUDA(dev_alloc((void**)&d_m, sizeof(int32_t) * T));
     LISA_CUDA(cudaMemcpyAsync(d_v, p.vertices, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice, r.stream));
     LISA_CUDA(cudaMemcpyAsync(d_n, p.normals, sizeof(float) * 9ull * T, cudaMemcpyHostToDevice, r.stream));
     LISA_CUDA(cudaMemcpyAsync(d_m, p.mat_indices, sizeof(int32_t) * T, cudaMemcpyHostToDevice, r.stream));
@@ -328,7 +430,7 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
     std::vector<int32_t> em(std::max(p.num_materials, 1), -1);
     for (int i = 0; i < p.num_materials; ++i) em[i] = p.materials[i].emit ? i : -1;
     int32_t* d_em = nullptr;
-    if (e == cudaSuccess) e = cudaMalloc(&d_em, sizeof(int32_t) * em.size());
+    if (e == cudaSuccess) e = dev_alloc((void**)&d_em, sizeof(int32_t) * em.size());
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d_em, em.data(), sizeof(int32_t) * em.size(), cudaMemcpyHostToDevice, r.stream);
     if (e == cudaSuccess) {
@@ -336,23 +438,26 @@ Status create_scene(Renderer& r, const lisa_renderer_params& p, SceneGpu& s) {
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);
-    if (d_em) cudaFree(d_em);
     if (e != cudaSuccess) {
-      cudaFree(d_v);
-      cudaFree(d_n);
-      cudaFree(d_m);
+      cudaDeviceSynchronize();  // before the blocks are reused
+      dev_free(d_em);
+      dev_free(d_v);
+      dev_free(d_n);
+      dev_free(d_m);
       return Status::cuda(e, "pack triangles");
     }
+    dev_free(d_em);
   }
   Status st;
   {
     TempDeviceBufs tmp;
+    tmp.stream = r.stream;
     st = build_bvh(d_v, T, r.stream, tmp, r.arena, &s.nodes, &s.tris, &s.bvh, d_m, r.opts.bvh_lbvh_only == 0);
     cudaStreamSynchronize(r.stream);
   }
-  if (d_v) cudaFree(d_v);
-  if (d_n) cudaFree(d_n);
-  if (d_m) cudaFree(d_m);
+  dev_free(d_v);
+  dev_free(d_n);
+  dev_free(d_m);
   LISA_TRY(st);
   const float dx = s.bvh.bmax[0] - s.bvh.bmin[0], dy = s.bvh.bmax[1] - s.bvh.bmin[1],
               dz = s.bvh.bmax[2] - s.bvh.bmin[2];
@@ -579,6 +684,14 @@ extern "C" {
 const char* lisa_last_error(void) { return g_last_error.c_str(); }
 
 const char* lisa_version(void) { return "lisa_gb300 1.0 (sm_103a)"; }
+
+int lisa_device_cache_release(uint64_t* bytes) {
+  API_GUARD({
+    const size_t n = dev_cache_release();
+    if (bytes) *bytes = n;
+    return ret(Status());
+  });
+}
 
 int lisa_device_info(int* sm_count, int* cc_major, int* cc_minor) {
   API_GUARD({

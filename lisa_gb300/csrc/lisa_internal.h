@@ -60,6 +60,17 @@ Status write_ppm_rgba8(const char* path, const uint8_t* rgba8, uint32_t w, uint3
 Status write_ppm_rgb8_flipped(const char* path, const uint8_t* rgb8, uint32_t w, uint32_t h);
 
 // ---- device memory sources ---------------------------------------------------
+// Device memory for the library's buffers.  Freed blocks are kept for
+// reuse (per device, up to a cap) instead of being returned with cudaFree:
+// cudaMalloc and cudaFree are synchronous and take milliseconds at the
+// renderer's sizes, which a create-render-destroy cycle pays every time.
+// A block may be freed only once the work that used it has finished (the
+// callers synchronise their stream first).  dev_alloc returns
+// cudaErrorMemoryAllocation after dropping the cache and retrying once.
+cudaError_t dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+size_t dev_cache_release();  // cudaFree every cached block; the bytes freed
+
 // Where a builder takes its device buffers from: cudaMalloc (DeviceArena,
 // TempDeviceBufs) or a caller-provided region (BumpScratch).
 struct ScratchSource {
@@ -81,6 +92,7 @@ struct DeviceArena : ScratchSource {
 // cudaMalloc'd temporaries freed when the object goes out of scope.
 struct TempDeviceBufs : ScratchSource {
   std::vector<void*> ptrs;
+  cudaStream_t stream = nullptr;  // the work using the buffers (null: the whole device)
   Status get(void** p, size_t bytes, const char* what) override;
   ~TempDeviceBufs() override;
 };

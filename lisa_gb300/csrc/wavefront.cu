@@ -1696,16 +1696,21 @@ Status renderer_get_image(Renderer& r, int scene, float* rgb32, uint8_t* rgba8, 
   const double n = (double)s.samples_done;
   float* d_rgb = nullptr;
   uchar4* d_rgba = nullptr;
-  if (rgb32 || var) LISA_CUDA(cudaMalloc(&d_rgb, sizeof(float) * 3 * std::max<uint32_t>(npix, 1)));
-  if (rgba8) LISA_CUDA(cudaMalloc(&d_rgba, sizeof(uchar4) * std::max<uint32_t>(npix, 1)));
+  if (rgb32 || var) LISA_CUDA(dev_alloc((void**)&d_rgb, sizeof(float) * 3 * std::max<uint32_t>(npix, 1)));
+  if (rgba8) LISA_CUDA(dev_alloc((void**)&d_rgba, sizeof(uchar4) * std::max<uint32_t>(npix, 1)));
   const float inv_n = n > 0 ? (float)(1.0 / n) : 0.0f;
   if (npix) {
     k_tonemap<<<r.sm_count * 4, 256, 0, r.stream>>>(s.acc_sum, npix, inv_n, s.params.width, s.params.height, d_rgb,
                                                      d_rgba, nullptr);
     LISA_CUDA(cudaGetLastError());
   }
+  // the mean goes straight to the caller's buffer unless the FP64 figures
+  // below need it on the host as well
+  const bool direct = rgb32 && !var && !mean64;
   std::vector<float> h_rgb;
-  if (d_rgb) {
+  if (d_rgb && direct) {
+    LISA_CUDA(cudaMemcpyAsync(rgb32, d_rgb, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, r.stream));
+  } else if (d_rgb) {
     h_rgb.resize(3ull * npix);
     LISA_CUDA(cudaMemcpyAsync(h_rgb.data(), d_rgb, sizeof(float) * 3 * npix, cudaMemcpyDeviceToHost, r.stream));
   }
@@ -1721,11 +1726,11 @@ Status renderer_get_image(Renderer& r, int scene, float* rgb32, uint8_t* rgba8, 
         cudaMemcpyAsync(m64.data(), s.acc_sum64, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, r.stream));
   }
   LISA_CUDA(cudaStreamSynchronize(r.stream));
-  if (d_rgb) cudaFree(d_rgb);
-  if (d_rgba) cudaFree(d_rgba);
+  dev_free(d_rgb);
+  dev_free(d_rgba);
   // The mean is the float Kahan sum over n (mean of the samples); rgb32 row 0
   // is the bottom row like the reference accum_buffer.
-  if (rgb32) std::memcpy(rgb32, h_rgb.data(), sizeof(float) * 3 * npix);
+  if (rgb32 && !direct) std::memcpy(rgb32, h_rgb.data(), sizeof(float) * 3 * npix);
   if (mean64) {
     if (s.acc_sum64) {
       for (size_t i = 0; i < 3ull * npix; ++i) mean64[i] = n > 0 ? m64[i] / n : 0.0;
@@ -1749,14 +1754,15 @@ Status renderer_get_ppm(Renderer& r, int scene, uint8_t* rgb8) {
   const uint32_t npix = s.npix;
   if (npix == 0) return Status();
   unsigned char* d = nullptr;
-  LISA_CUDA(cudaMalloc(&d, 3ull * npix));
+  LISA_CUDA(dev_alloc((void**)&d, 3ull * npix));
   const float inv_n = s.samples_done > 0 ? (float)(1.0 / (double)s.samples_done) : 0.0f;
   k_tonemap<<<r.sm_count * 4, 256, 0, r.stream>>>(s.acc_sum, npix, inv_n, s.params.width, s.params.height, nullptr,
                                                    nullptr, d);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(rgb8, d, 3ull * npix, cudaMemcpyDeviceToHost, r.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(r.stream);
-  cudaFree(d);
+  else cudaStreamSynchronize(r.stream);
+  dev_free(d);
   if (e != cudaSuccess) return Status::cuda(e, "ppm payload");
   return Status();
 }
