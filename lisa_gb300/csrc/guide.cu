@@ -78,17 +78,12 @@ __device__ __forceinline__ void pack_store(uint16_t* pack, int row, int col, flo
 // surrounds a step: the gradient is the sum of the training CTAs' partial
 // gradients, the BF16 forward and transposed copies of each updated weight
 // are written in place (the zero padding rows never change), and the summed
-// loss goes to loss_last.  The step count lives on the device (the training kernel
-// increments it), so a captured graph replays with the right bias
-// correction.  With `count`, the step is skipped when the training slice
-// that starts at `first` had no sample (a wave that gathered fewer samples
-// than its steps would use): momentum alone would keep moving the weights.
+// loss goes to loss_last.  The step count lives on the device (the training
+// kernel increments it).
 __global__ void k_guide_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
                              const float* __restrict__ part, const float* __restrict__ loss_part, uint32_t nparts,
                              float* __restrict__ loss_last, float lr, const uint32_t* __restrict__ step,
-                             uint32_t* status, uint16_t* __restrict__ pack, const uint32_t* __restrict__ count,
-                             uint32_t first) {
-  if (count && *(volatile const uint32_t*)count <= first) return;
+                             uint32_t* status, uint16_t* __restrict__ pack) {
   // four threads per parameter (neighbouring lanes) each sum every fourth
   // partial slot; the sums meet by shuffles
   const int t4 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -377,8 +372,7 @@ template <int SRC>
 __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restrict__ pack, const float* __restrict__ master,
                                                         GuideSrc src, float inv_n, float* __restrict__ part,
                                                         float* __restrict__ loss_part, uint32_t* status,
-                                                        uint32_t* __restrict__ step_bump,
-                                                        unsigned long long* __restrict__ sample_count) {
+                                                        uint32_t* __restrict__ step_bump) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = align1024(smem_raw);
   uint8_t* w = smem;
@@ -396,7 +390,6 @@ __global__ void __launch_bounds__(128, 1) k_guide_train(const uint16_t* __restri
   const uint32_t ntiles = (n - src.first + 127) / 128;
   // the Adam step that follows (none for an empty slice)
   if (step_bump && n > src.first && blockIdx.x == 0 && threadIdx.x == 0) *step_bump += 1;
-  if (sample_count && n > src.first && blockIdx.x == 0 && threadIdx.x == 0) *sample_count += n - src.first;
   float* slot = part + (size_t)blockIdx.x * NPARAM;  // this CTA's partial gradient
   if (blockIdx.x >= ntiles) {
     for (int k = threadIdx.x; k < NPARAM; k += blockDim.x) slot[k] = 0.0f;
@@ -756,7 +749,6 @@ Status guide_create(uint32_t seed, std::unique_ptr<GuideNet>& out, cudaStream_t 
   static bool attr_set = false;
   if (!attr_set) {
     LISA_CUDA(cudaFuncSetAttribute(k_guide_train<SRC_RAW>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM));
-    LISA_CUDA(cudaFuncSetAttribute(k_guide_train<SRC_GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM));
     LISA_CUDA(cudaFuncSetAttribute(k_guide_infer<SRC_RAW>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM));
     LISA_CUDA(cudaFuncSetAttribute(k_guide_infer<SRC_NEE>, cudaFuncAttributeMaxDynamicSharedMemorySize, INFER_SMEM));
     attr_set = true;
@@ -780,19 +772,15 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
 // loss to its own slot of g.grad_part / g.loss_part (no atomics); the Adam
 // step (or guide_launch_reduce) sums them.  With adam_follows the device
 // step count advances for the Adam step launched next.
-Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s, bool adam_follows, unsigned long long* sample_count) {
+Status guide_launch_train(GuideNet& g, const GuideSrc& src, float inv_n, uint32_t max_n, cudaStream_t s,
+                          bool adam_follows) {
   if (!g.grad_part) return Status::invalid("guide: no partial-gradient slots");
   const uint32_t tiles = std::max<uint32_t>(1, (max_n + 127) / 128);
   const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count_current());
   g.nparts = grid;
   uint32_t* bump = adam_follows ? g.d_step : nullptr;
-  if (src_kind == SRC_RAW)
-    k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
-                                                         g.status, bump, sample_count);
-  else
-    k_guide_train<SRC_GEOM><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
-                                                          g.status, bump, sample_count);
+  k_guide_train<SRC_RAW><<<grid, 128, TRAIN_SMEM, s>>>(g.w_bf16, g.master, src, inv_n, g.grad_part, g.loss_part,
+                                                       g.status, bump);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
@@ -841,9 +829,9 @@ Status guide_launch_reduce(GuideNet& g, cudaStream_t s) {
   return Status();
 }
 
-Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s, const uint32_t* count, uint32_t first) {
+Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s) {
   k_guide_adam<<<(4 * NPARAM + 255) / 256, 256, 0, s>>>(g.master, g.adam_m, g.adam_v, g.grad_part, g.loss_part, g.nparts,
-                                                    g.loss_last, lr, g.d_step, g.status, g.w_bf16, count, first);
+                                                    g.loss_last, lr, g.d_step, g.status, g.w_bf16);
   LISA_CUDA(cudaGetLastError());
   return Status();
 }
@@ -1028,7 +1016,7 @@ int lisa_guide_train_step(lisa_guide* g, const float* features, const float* dir
     src.dirs = d_d;
     src.weights = d_w;
     src.n = n;
-    LISA_TRY(guide_launch_train(g->get(), src, SRC_RAW, 1.0f / (float)n, n, g->stream, lr > 0.0f));
+    LISA_TRY(guide_launch_train(g->get(), src, 1.0f / (float)n, n, g->stream, lr > 0.0f));
     LISA_TRY(guide_launch_reduce(g->get(), g->stream));
     if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->get().loss, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     if (grads)

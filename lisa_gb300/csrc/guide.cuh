@@ -65,11 +65,11 @@ Status guide_collect(Renderer& r, int wave, uint32_t cap, cudaStream_t s);
 // outputs: max_n x 40 floats (entries beyond the live count are not written)
 Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float* out, uint32_t max_n,
                           cudaStream_t s);
-// one training launch: each CTA writes its partial gradient and loss to its
-// slot; with adam_follows the device step count advances for the next Adam
-// step; sample_count (optional) accumulates the samples trained on
-Status guide_launch_train(GuideNet& g, const GuideSrc& src, int src_kind, float inv_n, uint32_t max_n,
-                          cudaStream_t s, bool adam_follows, unsigned long long* sample_count = nullptr);
+// one training launch on RAW samples (the guide's own C ABI): each CTA
+// writes its partial gradient and loss to its slot; with adam_follows the
+// device step count advances for the next Adam step
+Status guide_launch_train(GuideNet& g, const GuideSrc& src, float inv_n, uint32_t max_n, cudaStream_t s,
+                          bool adam_follows);
 // Up to `rounds` Adam steps on slices of `chunk` samples of src (RAW or
 // GEOM), in one cooperative launch; acc is scratch of
 // guide_train_acc_words() floats
@@ -80,8 +80,7 @@ size_t guide_train_acc_words();
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s);
 // Adam step on the summed partials; also refreshes the BF16 weights and
 // moves the loss to loss_last
-// With `count`: skipped on the device when the slice starting at `first` is empty.
-Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s, const uint32_t* count = nullptr, uint32_t first = 0);
+Status guide_launch_adam(GuideNet& g, float lr, cudaStream_t s);
 Status guide_check_status(GuideNet& g, cudaStream_t s);
 Status guide_renderer_init(Renderer& r);
 // Shared-memory attributes of the renderer's fused inference kernels (wavefront.cu).

@@ -149,6 +149,36 @@ def test_cuda_graph_replay_matches_stream_launches(gpu):
     assert np.array_equal(a.image(), b.image())
 
 
+def test_reused_device_memory_gives_the_same_image(gpu):
+    """Renderers created after others were destroyed take their buffers from
+    the device-memory cache (blocks that still hold the old contents); the
+    images are the same, bit for bit, as from a renderer on fresh memory,
+    and lisa_device_cache_release hands the cached blocks back."""
+    import ctypes as C
+
+    lib = L._native.lib()
+    freed = C.c_uint64()
+    L._native.check(lib.lisa_device_cache_release(C.byref(freed)))
+    icos = scenes.icosphere_box(level=4, width=64, height=48, num_samples=8, num_bounces=6)
+    box = scenes.cornell_box(width=64, height=48, num_samples=8, num_bounces=6)
+    first = L.Renderer(L.params_from_scene(icos), seed=5)
+    first.render()
+    want = first.image()
+    first.close()
+    for other in (box, icos):  # the cached blocks now hold another scene's state
+        r = L.Renderer(L.params_from_scene(other), seed=9)
+        r.render()
+        r.close()
+    again = L.Renderer(L.params_from_scene(icos), seed=5)
+    again.render()
+    assert np.array_equal(again.image(), want)
+    again.close()
+    L._native.check(lib.lisa_device_cache_release(C.byref(freed)))
+    assert freed.value > 0
+    L._native.check(lib.lisa_device_cache_release(C.byref(freed)))
+    assert freed.value == 0
+
+
 def test_wave_splitting_small_capacity(gpu):
     """A capacity smaller than one image plane splits planes into pixel
     ranges; the result is unchanged."""
