@@ -369,7 +369,15 @@ __global__ void k_bottom_up(uint32_t n, const uint32_t* __restrict__ vals, const
 constexpr float SAH_CI = 1.2f;  // cost of a node visit relative to a triangle test
 constexpr float SAH_CT = 1.0f;
 constexpr int TL = 7;           // treelet leaves
-constexpr uint32_t TREELET_MIN_PRIMS = 16;  // smaller subtrees keep their LBVH topology (the 8-wide collapse flattens them)
+// Subtrees of fewer primitives keep their LBVH topology (the 8-wide
+// collapse flattens them).  Measured on the 1.31 M-triangle icosphere box
+// and the 4.48 M-triangle sphere soup: 64 against 16 builds in 3.8 instead
+// of 5.1 ms and 6.9 instead of 10.7 ms, with the same Mrays/s on the first
+// and 0.4 % fewer on the second.
+#ifndef LISA_TREELET_MIN_PRIMS
+#define LISA_TREELET_MIN_PRIMS 64
+#endif
+constexpr uint32_t TREELET_MIN_PRIMS = LISA_TREELET_MIN_PRIMS;
 
 __device__ __forceinline__ float4 box_min(float4 a, float4 b) {
   return make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), 0.0f);
