@@ -209,7 +209,7 @@ struct Renderer {
   uint32_t graph_launches[5] = {0, 0, 0, 0, 0};  // trace, shade, nee, total, guide
   // guided mode
   std::vector<std::unique_ptr<GuideNet>> guides;
-  float4* rec_list = nullptr;    // rec_cap kept training records (5 float4 each)
+  float4* rec_list = nullptr;    // rec_cap kept training records (4 float4 each, then rec_cap float4: rec_col)
   uint32_t rec_cap = 0;
   float4* nee_light = nullptr;   // guided physically based mode: capacity x 2 emitter samples
   float4* guide_batch = nullptr; // guide_batch_cap x 4 training samples

@@ -678,12 +678,12 @@ __device__ __forceinline__ uint32_t record_reserve(const WaveBufs& b, int depth,
 __device__ __forceinline__ void record_write(const WaveBufs& b, uint32_t k, uint32_t slot, float flag, float4 r0,
                                              float4 r1, float4 r2, float4 r3, V3 c0) {
   if (k == ~0u) return;
-  float4* rec = b.rec_list + 5ull * k;
+  float4* rec = b.rec_list + 4ull * k;
   rec[0] = r0;
   rec[1] = r1;
   rec[2] = r2;
   rec[3] = r3;
-  rec[4] = make_float4(c0.x, c0.y, c0.z, __uint_as_float((slot << 1) | (flag != 0.0f ? 1u : 0u)));
+  b.rec_col[k] = make_float4(c0.x, c0.y, c0.z, __uint_as_float((slot << 1) | (flag != 0.0f ? 1u : 0u)));
 }
 
 // ---------------------------------------------------------------------------
@@ -1059,20 +1059,25 @@ __global__ void k_guide_collect(WaveBufs b, float4* __restrict__ batch, uint32_t
     float4 r0, r1, r2, r3, r4;
     float wt = 0.0f;
     if (k < nrec) {
-      const float4* rec = b.rec_list + 5ull * k;
-      r0 = rec[0];
-      r1 = rec[1];
-      r2 = rec[2];
-      r3 = rec[3];
-      r4 = rec[4];
+      r4 = b.rec_col[k];
       const float4 col = b.ps_col[__float_as_uint(r4.w) >> 1];
-      float l = 0.0f;
-      int nl = 0;
-      if (r3.x > 0.0f) { l += (col.x - r4.x) / r3.x; ++nl; }
-      if (r3.y > 0.0f) { l += (col.y - r4.y) / r3.y; ++nl; }
-      if (r3.z > 0.0f) { l += (col.z - r4.z) / r3.z; ++nl; }
-      wt = nl ? l / (float)nl * r0.w : 0.0f;
-      want = wt > 0.0f && isfinite(wt);
+      // no channel gained radiance after the vertex: every term below is
+      // <= 0 (or not a number), so the record is not wanted -- its other
+      // four float4 are not read
+      if (col.x > r4.x || col.y > r4.y || col.z > r4.z) {
+        const float4* rec = b.rec_list + 4ull * k;
+        r0 = rec[0];
+        r1 = rec[1];
+        r2 = rec[2];
+        r3 = rec[3];
+        float l = 0.0f;
+        int nl = 0;
+        if (r3.x > 0.0f) { l += (col.x - r4.x) / r3.x; ++nl; }
+        if (r3.y > 0.0f) { l += (col.y - r4.y) / r3.y; ++nl; }
+        if (r3.z > 0.0f) { l += (col.z - r4.z) / r3.z; ++nl; }
+        wt = nl ? l / (float)nl * r0.w : 0.0f;
+        want = wt > 0.0f && isfinite(wt);
+      }
     }
     const uint32_t i = warp_reserve(&b.ctrl->train_count, want);
     if (want && i < cap) {
@@ -1309,6 +1314,7 @@ WaveBufs make_bufs(Renderer& r) {
   b.refill_busy_max = 32u - (r.opts.refill_idle ? std::min<uint32_t>(r.opts.refill_idle, 32u) : LISA_REFILL_IDLE);
   b.physical = r.opts.estimator == LISA_ESTIMATOR_PHYSICAL;
   b.rec_list = r.rec_list;
+  b.rec_col = r.rec_list ? r.rec_list + 4ull * r.rec_cap : nullptr;
   b.rec_cap = r.rec_cap;
   b.nee_light = r.nee_light;
   b.bsdf_fraction = r.opts.guide_bsdf_fraction;

@@ -24,17 +24,22 @@ struct WaveBufs {
   uint32_t refill_busy_max;  // persistent kernels refill a warp once at most this many lanes are busy
   uint32_t physical;         // physically based estimator: ps_att.w = pdf of the last diffuse bounce
   // guided mode (null otherwise)
-  float4* rec_list;   // kept training records, 5 float4 each (see below)
+  float4* rec_list;   // kept training records, 4 float4 each (see below)
+  float4* rec_col;    // and their fifth float4, in an array of its own
   uint32_t rec_cap;   // records rec_list holds
   uint32_t rec_salt;  // per-wave salt of the keep decision
   float4* nee_light;  // guided physically based mode: per entry, the emitter sample (2 float4)
   float bsdf_fraction;  // one-sample MIS: probability of the BSDF strategy
 };
 
-// Training record of one kept guided vertex (5 float4, appended to rec_list):
+// Training record of one kept guided vertex, appended to rec_list:
 //   (p.xyz, weight = p_bsdf/q)  (N.xyz, w.x)  (view.xyz, w.y)
 //   (throughput after the bounce .xyz, w.z)
+// and, at the same index of rec_col,
 //   (radiance so far .xyz, bits: slot << 1 | emitter flag)
+// -- what the collection reads first to learn whether the path gathered
+// radiance after the vertex (most do not, and their other 64 B are never
+// read).
 
 struct GuideSampling {
   float bsdf_fraction;  // c in q = c p_bsdf + (1-c) p_guide
