@@ -68,7 +68,17 @@ struct Lobe {
   float nk;          // vMF normalisation kappa / (2 pi (1 - e^{-2 kappa}))
 };
 
-// Decodes the 40 raw outputs: per lobe (mu xyz, kappa, logit).
+// 1 - e^{-t} for t >= 0: a three-term series below 0.05 (relative error
+// under 1e-6 there), else 1 - __expf(-t) (its cancellation costs at most
+// 5 bits at t = 0.05).
+__device__ __forceinline__ float one_minus_exp_neg(float t) {
+  return t < 0.05f ? t * (1.0f - t * (0.5f - t * (1.0f / 6.0f))) : 1.0f - __expf(-t);
+}
+
+// Decodes the 40 raw outputs: per lobe (mu xyz, kappa, logit).  Fast
+// intrinsics throughout: sampling and density read the same decoded lobes,
+// so their small errors change which mixture is used, not the estimator's
+// expectation.
 __device__ __forceinline__ void decode(const float* o, Lobe* L) {
   float mx = -1e30f;
 #pragma unroll
@@ -80,20 +90,20 @@ __device__ __forceinline__ void decode(const float* o, Lobe* L) {
     L[k].w = e;
     z += e;
   }
-  const float iz = 1.0f / z;
+  const float iz = __fdividef(1.0f, z);
 #pragma unroll
   for (int k = 0; k < LOBES; ++k) {
     const float ax = o[5 * k], ay = o[5 * k + 1], az = o[5 * k + 2];
-    const float n = fmaxf(sqrtf(ax * ax + ay * ay + az * az), 1e-6f);
-    const float in = 1.0f / n;
+    const float n2 = fmaxf(ax * ax + ay * ay + az * az, 1e-12f);
+    const float in = rsqrtf(n2);
     L[k].mx = ax * in;
     L[k].my = ay * in;
     L[k].mz = az * in;
-    L[k].norm = n;
+    L[k].norm = n2 * in;
     const float kap = __expf(fminf(fmaxf(o[5 * k + 3], KAPPA_LO), KAPPA_HI));
     L[k].kappa = kap;
-    // 1 - e^{-2k} = -expm1(-2k); once per lobe, not per evaluation
-    L[k].nk = kap / (6.28318530717958647692f * -expm1f(-2.0f * kap));
+    // the vMF normalisation, once per lobe, not per evaluation
+    L[k].nk = __fdividef(kap, 6.28318530717958647692f * one_minus_exp_neg(2.0f * kap));
     L[k].w *= iz;
   }
 }
@@ -129,7 +139,7 @@ __device__ __forceinline__ void mix_sample(const Lobe* L, float u0, float u1, fl
   const float k = l.kappa;
   // cos of the angle to mu: 1 + log(u1 + (1-u1) e^{-2k}) / k  (kappa <= e^5
   // keeps e^{-2k} representable enough; the clamp guards u1 = 0)
-  const float ww = fminf(fmaxf(1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * k)) / k, -1.0f), 1.0f);
+  const float ww = fminf(fmaxf(1.0f + __fdividef(__logf(u1 + (1.0f - u1) * __expf(-2.0f * k)), k), -1.0f), 1.0f);
   const float st = sqrtf(fmaxf(0.0f, 1.0f - ww * ww));
   float sp, cp;
   sincospif(2.0f * u2, &sp, &cp);
@@ -150,7 +160,7 @@ __device__ __forceinline__ void mix_sample(const Lobe* L, float u0, float u1, fl
 __device__ __forceinline__ float hemi_pdf(float nx, float ny, float nz, float wx, float wy, float wz) {
   if (nx * wx + ny * wy + nz * wz <= 0.0f) return 0.0f;
   const float m = fmaxf(fabsf(wx), fmaxf(fabsf(wy), fabsf(wz)));
-  return 1.0f / (12.0f * m * m * m);
+  return __fdividef(1.0f, 12.0f * m * m * m);
 }
 
 // Gradient of  -wt * log q(w)  with respect to the 40 raw outputs o; also
