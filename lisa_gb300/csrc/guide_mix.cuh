@@ -34,11 +34,12 @@ __device__ __forceinline__ void encode(const float* bmin, const float* bmax, flo
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float ext = bmax[a] - bmin[a];
-    const float u = ext > 0.0f ? fminf(fmaxf((p[a] - bmin[a]) / ext, 0.0f), 1.0f) : 0.5f;
-    // one sincospi, then the double-angle recurrence for the higher octaves
-    // (error ~2^k ulp at octave k: far below the inputs' BF16 precision)
+    const float u = ext > 0.0f ? fminf(fmaxf(__fdividef(p[a] - bmin[a], ext), 0.0f), 1.0f) : 0.5f;
+    // one fast sine/cosine (absolute error ~2^-21 on [0, pi/8]), then the
+    // double-angle recurrence for the higher octaves (the error doubles per
+    // octave: ~2^-10 at the last, still under the inputs' BF16 precision)
     float sn, cs;
-    sincospif(u * 0.125f, &sn, &cs);
+    __sincosf(u * 0.39269908169872414f, &sn, &cs);
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
       f[3 * k + a] = sn;

@@ -910,10 +910,12 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, f
   if (l1.z != 0.0f) {
     const float pl = l0.w, cos_x = l1.x;
     const DevMaterial& em = sc.mats[__float_as_int(l1.y)];
-    const float fcos = fmul(r, fdiv(cos_x, PI_F));
-    const float pb = r * (c * (cos_x / PI_F) + (1.0f - c) * guide::mix_pdf(L, l0.x, l0.y, l0.z));
-    const float wl = (pl * pl) / (pl * pl + pb * pb);
-    col = col + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * fdiv(fcos, pl)) * wl;
+    // (fast reciprocals: the guided bounce's densities need no bit-exact
+    // agreement with the oracle, only the same values for sampling and weight)
+    const float fcos = r * cos_x * (1.0f / PI_F);
+    const float pb = r * (c * (cos_x * (1.0f / PI_F)) + (1.0f - c) * guide::mix_pdf(L, l0.x, l0.y, l0.z));
+    const float wl = __fdividef(pl * pl, pl * pl + pb * pb);
+    col = col + ((att * v3(em.emission[0], em.emission[1], em.emission[2])) * __fdividef(fcos, pl)) * wl;
   }
   float prev = 0.0f;
   bool want;
@@ -925,9 +927,9 @@ __device__ __forceinline__ bool guided_pb_vertex(const WaveBufs& b, int depth, f
       guide::mix_sample(L, u0, u1, u2, nd.x, nd.y, nd.z);
     }
     const float cs = dot(Ns, nd);
-    const float pc = cs > 0.0f ? cs / PI_F : 0.0f;
+    const float pc = cs > 0.0f ? cs * (1.0f / PI_F) : 0.0f;
     const float qm = c * pc + (1.0f - c) * guide::mix_pdf(L, nd.x, nd.y, nd.z);
-    const float weight = (pc > 0.0f && qm > 0.0f && isfinite(qm)) ? pc / qm : 0.0f;
+    const float weight = (pc > 0.0f && qm > 0.0f && isfinite(qm)) ? __fdividef(pc, qm) : 0.0f;
     att = att * weight;
     prev = r * qm;
     want = weight > 0.0f;
