@@ -5,6 +5,8 @@
 // the GPU instead of optixAccelBuild (:92-145), the camera frame is the SDK
 // camera's UVW frame (src/sutil/Camera.cpp:34-45, set up in init_params
 // :434-442), and the launch state becomes the wavefront buffers.
+#include <cuda.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -46,17 +48,48 @@ static int ret(const Status& s) {
     return ret(Status(LISA_ERR_INVALID, "unknown error"));  \
   }
 
+// ---- CUDA context identity -------------------------------------------------
+using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique ID of the current CUDA context (the driver API through the
+// runtime's entry-point query, so the library needs no libcuda link).
+// *none is set when no context is current yet.
+Status current_context_id(unsigned long long* id, bool* none) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    LISA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
+    LISA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return Status(LISA_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
+    get_current = (PfnCtxGetCurrent)f1;
+    get_id = (PfnCtxGetId)f2;
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return Status(LISA_ERR_CUDA, "cuCtxGetCurrent failed");
+  *none = ctx == nullptr;
+  if (*none) return Status();
+  if (get_id(ctx, id) != CUDA_SUCCESS) return Status(LISA_ERR_CUDA, "cuCtxGetId failed");
+  return Status();
+}
+
 // ---- device memory cache -----------------------------------------------------
 // Blocks are rounded up to 64 KiB (2 MiB above 32 MiB); a request takes the
-// smallest cached block of its device that is at least as large and at most
-// 1/8 + 2 MiB larger.  The cache holds at most LISA_DEVICE_CACHE_MB (default
+// smallest cached block of the current CUDA context that is at least as
+// large and at most 1/8 + 2 MiB larger.  Blocks are keyed by context ID, not
+// device ordinal: a context the application creates, or the primary context
+// after a device reset, never receives another context's addresses.  The cache holds at most LISA_DEVICE_CACHE_MB (default
 // 8192; 0 turns it off) of free blocks per process.  The state is never
 // destroyed (no CUDA call from a static destructor at process exit).
 namespace {
 struct DevCache {
   std::mutex mu;
-  std::unordered_map<void*, std::pair<size_t, int>> live;  // block -> (rounded size, device)
-  std::multimap<std::pair<int, size_t>, void*> free_blocks;
+  std::unordered_map<void*, std::pair<size_t, unsigned long long>> live;  // block -> (rounded size, context)
+  std::multimap<std::pair<unsigned long long, size_t>, void*> free_blocks;
   size_t free_bytes = 0;
   size_t cap = 0;
   DevCache() {
@@ -64,11 +97,16 @@ struct DevCache {
     cap = (size_t)(v ? std::strtoull(v, nullptr, 10) : 8192ull) << 20;
   }
   void release_locked() {
-    for (auto& kv : free_blocks) cudaFree(kv.second);
+    // (blocks of a context that is not current, or no longer exists, fail
+    // to free; their records are dropped all the same)
+    for (auto& kv : free_blocks)
+      if (cudaFree(kv.second) != cudaSuccess) cudaGetLastError();
     free_blocks.clear();
     free_bytes = 0;
   }
 };
+constexpr unsigned long long NO_CTX = ~0ull;  // a block's context was not known
+
 DevCache& dev_cache() {
   static DevCache* c = new DevCache();
   return *c;
@@ -82,28 +120,32 @@ size_t dev_round(size_t bytes) {
 
 cudaError_t dev_alloc(void** p, size_t bytes) {
   DevCache& c = dev_cache();
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
+  unsigned long long ctx = 0;
+  bool none = true;
+  if (!current_context_id(&ctx, &none).ok()) none = true;  // then nothing is reused
   const size_t need = dev_round(bytes);
   std::lock_guard<std::mutex> lock(c.mu);
-  auto it = c.free_blocks.lower_bound({dev, need});
-  if (it != c.free_blocks.end() && it->first.first == dev && it->first.second <= need + need / 8 + (2ull << 20)) {
-    *p = it->second;
-    c.live[it->second] = {it->first.second, dev};
-    c.free_bytes -= it->first.second;
-    c.free_blocks.erase(it);
-    return cudaSuccess;
+  if (!none) {
+    auto it = c.free_blocks.lower_bound({ctx, need});
+    if (it != c.free_blocks.end() && it->first.first == ctx && it->first.second <= need + need / 8 + (2ull << 20)) {
+      *p = it->second;
+      c.live[it->second] = {it->first.second, ctx};
+      c.free_bytes -= it->first.second;
+      c.free_blocks.erase(it);
+      return cudaSuccess;
+    }
   }
   void* q = nullptr;
-  e = cudaMalloc(&q, need);
+  cudaError_t e = cudaMalloc(&q, need);
   if (e == cudaErrorMemoryAllocation && !c.free_blocks.empty()) {
     cudaGetLastError();
     c.release_locked();
     e = cudaMalloc(&q, need);
   }
   if (e != cudaSuccess) return e;
-  c.live[q] = {need, dev};
+  if (none && !current_context_id(&ctx, &none).ok()) none = true;  // cudaMalloc made one current
+  // a block whose context is unknown is freed, not cached
+  c.live[q] = {need, none ? NO_CTX : ctx};
   *p = q;
   return cudaSuccess;
 }
@@ -118,10 +160,10 @@ void dev_free(void* p) {
     return;
   }
   const size_t bytes = it->second.first;
-  const int dev = it->second.second;
+  const unsigned long long ctx = it->second.second;
   c.live.erase(it);
-  if (c.free_bytes + bytes <= c.cap) {
-    c.free_blocks.insert({{dev, bytes}, p});
+  if (ctx != NO_CTX && c.free_bytes + bytes <= c.cap) {
+    c.free_blocks.insert({{ctx, bytes}, p});
     c.free_bytes += bytes;
   } else {
     cudaFree(p);

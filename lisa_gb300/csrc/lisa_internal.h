@@ -67,6 +67,8 @@ Status write_ppm_rgb8_flipped(const char* path, const uint8_t* rgb8, uint32_t w,
 // A block may be freed only once the work that used it has finished (the
 // callers synchronise their stream first).  dev_alloc returns
 // cudaErrorMemoryAllocation after dropping the cache and retrying once.
+// Unique ID of the current CUDA context (*none when no context is current).
+Status current_context_id(unsigned long long* id, bool* none);
 cudaError_t dev_alloc(void** p, size_t bytes);
 void dev_free(void* p);
 size_t dev_cache_release();  // cudaFree every cached block; the bytes freed

@@ -57,34 +57,6 @@ std::mutex g_mu;
 ScratchEntry g_scratch[MAX_CONTEXTS] = {};
 int g_scratch_used = 0, g_scratch_next = 0;
 
-using PfnCtxGetCurrent = CUresult (*)(CUcontext*);
-using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long*);
-
-// Unique ID of the current CUDA context (the driver API through the
-// runtime's entry-point query, so the library needs no libcuda link).
-// *none is set when no context is current yet.
-Status current_context_id(unsigned long long* id, bool* none) {
-  static PfnCtxGetCurrent get_current = nullptr;
-  static PfnCtxGetId get_id = nullptr;
-  if (!get_current || !get_id) {
-    void* f1 = nullptr;
-    void* f2 = nullptr;
-    cudaDriverEntryPointQueryResult q1, q2;
-    LISA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1));
-    LISA_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
-    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
-      return Status(LISA_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
-    get_current = (PfnCtxGetCurrent)f1;
-    get_id = (PfnCtxGetId)f2;
-  }
-  CUcontext ctx = nullptr;
-  if (get_current(&ctx) != CUDA_SUCCESS) return Status(LISA_ERR_CUDA, "cuCtxGetCurrent failed");
-  *none = ctx == nullptr;
-  if (*none) return Status();
-  if (get_id(ctx, id) != CUDA_SUCCESS) return Status(LISA_ERR_CUDA, "cuCtxGetId failed");
-  return Status();
-}
-
 // Device address of the scratch array in the current context (looked up
 // once per context).
 Status scratch_address(void** out) {
