@@ -602,7 +602,8 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
       const uint32_t pq = p0 + 4u * (tid >> 2);
       float4 g4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (pq < (uint32_t)NPARAM) {
-#pragma unroll 8
+        // (sixteen slots in flight per thread: the sum is latency-bound)
+#pragma unroll 16
         for (uint32_t j = qq; j < gridDim.x; j += 4) {
           const float4 x = __ldcg(reinterpret_cast<const float4*>(part + (size_t)j * NPARAM + pq));
           g4.x += x.x;
