@@ -248,6 +248,13 @@ int lisa_render(lisa_renderer* r, lisa_render_stats* stats);
  * mean.  Replaces the display loop's launchSubframe + lerp
  * (render.cc:35-58,75-131; shader.cu:160-164) without the GL window. */
 int lisa_render_progressive(lisa_renderer* r, uint32_t spp, lisa_render_stats* stats);
+/* One call for a batch of scenes: creates a renderer over all of them
+ * (lisa_renderer_create_batch), renders num_samples per pixel for each
+ * (lisa_render), writes every scene with an output_image path to it as a
+ * PPM, and destroys the renderer.  stats (may be NULL) covers the render.
+ * What render() (render.cc:133-148) does for one scene, for many. */
+int lisa_batch_render(const lisa_renderer_params* scenes, int32_t num_scenes, const lisa_options* opts,
+                      lisa_render_stats* stats);
 /* Forget the accumulated samples (and, in guided mode, keep the guide). */
 int lisa_reset_accumulation(lisa_renderer* r);
 /* Index of the next sample of scene `scene` (LISA_RNG_PER_SAMPLE streams are

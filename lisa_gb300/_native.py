@@ -152,6 +152,7 @@ SIGNATURES = {
     "lisa_guide_set_params": (C.c_int, [_P, _P]),
     "lisa_guide_forward": (C.c_int, [_P, _P, C.c_uint32, _P]),
     "lisa_guide_train_step": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.c_float, _P, _P]),
+    "lisa_batch_render": (C.c_int, [_P, C.c_int32, _P, _P]),
     "lisa_guide_train_steps": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, _P]),
     "lisa_renderer_guide": (C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
 }

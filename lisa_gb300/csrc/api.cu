@@ -849,6 +849,25 @@ int lisa_render(lisa_renderer* r, lisa_render_stats* stats) {
   })
 }
 
+int lisa_batch_render(const lisa_renderer_params* scenes, int32_t n, const lisa_options* opts,
+                      lisa_render_stats* stats) {
+  API_GUARD({
+    Renderer* raw = nullptr;
+    Status s = renderer_create(scenes, n, opts, &raw);
+    if (!s.ok()) return ret(s);
+    std::unique_ptr<Renderer> r(raw);
+    s = renderer_render(*r, 0, false, stats);
+    for (int i = 0; s.ok() && i < n; ++i) {
+      SceneGpu& sg = r->scenes[i];
+      if (sg.output_image.empty()) continue;
+      std::vector<uint8_t> rgb(3ull * sg.npix);
+      s = renderer_get_ppm(*r, i, rgb.data());
+      if (s.ok()) s = write_ppm_rgb8_flipped(sg.output_image.c_str(), rgb.data(), sg.params.width, sg.params.height);
+    }
+    return ret(s);
+  })
+}
+
 int lisa_render_progressive(lisa_renderer* r, uint32_t spp, lisa_render_stats* stats) {
   API_GUARD({
     if (!r) return ret(Status::invalid("null renderer"));

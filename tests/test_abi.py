@@ -52,10 +52,10 @@ def test_errors_without_gpu_are_reported_not_raised():
     assert lib.lisa_render(None, None) == N.LISA_ERR_INVALID
     assert lib.lisa_selftest_wait_timeout(0, None) == N.LISA_ERR_INVALID
     assert lib.lisa_guide_train_steps(None, None, None, None, 0, 128, 1, 0.01, None) == N.LISA_ERR_INVALID
-    # nothing cached before any renderer ran
+    # the device-memory cache empties (without a GPU it never held anything)
     freed = C.c_uint64(123)
-    assert lib.lisa_device_cache_release(C.byref(freed)) == N.LISA_OK and freed.value == 0
     assert lib.lisa_device_cache_release(None) == N.LISA_OK
+    assert lib.lisa_device_cache_release(C.byref(freed)) == N.LISA_OK and freed.value == 0
 
 
 def test_renderer_options_are_checked_before_the_device():

@@ -175,6 +175,30 @@ def test_batch_of_uneven_scenes_matches_single_renders(gpu, estimator):
         assert np.array_equal(batch.image(k), single.image()), k
 
 
+def test_batch_render_one_call_writes_every_scene(gpu, tmp_path):
+    """lisa_batch_render: one call renders a batch of uneven scenes and
+    writes each scene's PPM to its output_image path -- the same bytes as
+    a batch renderer's save_image."""
+    import ctypes as C
+
+    a = scenes.cornell_box(width=32, height=24, num_samples=4, num_bounces=5)
+    b = scenes.icosphere_box(level=3, width=20, height=16, num_samples=8, num_bounces=6)
+    pa = L.params_from_scene(a, output_image=str(tmp_path / "a.ppm"))
+    pb = L.params_from_scene(b, output_image=str(tmp_path / "b.ppm"))
+    arr = (L._native.RendererParams * 2)(pa.raw, pb.raw)
+    opts = L.default_options(seed=3)
+    st = L._native.RenderStats()
+    L._native.check(L._native.lib().lisa_batch_render(C.cast(arr, C.c_void_p), 2, C.cast(C.byref(opts), C.c_void_p),
+                                                      C.cast(C.byref(st), C.c_void_p)))
+    assert st.rays_primary == 32 * 24 * 4 + 20 * 16 * 8
+    r = L.Renderer([pa, pb], opts)
+    r.render()
+    for k, name in enumerate(("a", "b")):
+        want = tmp_path / f"{name}_want.ppm"
+        r.save_image(str(want), scene=k)
+        assert (tmp_path / f"{name}.ppm").read_bytes() == want.read_bytes()
+
+
 def test_cuda_graph_replay_matches_stream_launches(gpu):
     """The captured graph (reused across calls with the same wave shape,
     fresh wave table each call) gives the same image as direct launches."""
