@@ -478,19 +478,16 @@ __device__ __forceinline__ bool grid_barrier(uint32_t* counter, uint32_t k, uint
 // One wave's training rounds in one cooperative launch (one CTA per SM, all
 // resident): for each slice of `chunk` samples [s * chunk, (s + 1) * chunk)
 // of the batch (while the batch has samples), every CTA
-//   1. reads the current weights and biases (loads that bypass L1: other
-//      CTAs wrote them in the last round),
+//   1. reads the current weights (a bulk copy behind a proxy fence) and
+//      biases (loads that bypass L1): other CTAs wrote them last round,
 //   2. runs its tiles of the slice (forward, loss gradient, backward),
-//   3. adds its dW, db and loss into acc (float atomics),
 //   3. writes its dW, db and loss to its own slot of part / loss_part,
 // the grid meets, CTA c sums the slots over its share of 128 parameters
 // (the same order as k_guide_adam: deterministic) and applies Adam to
 // them, refreshing their FP32 master and BF16 forward / transposed copies,
 // and the grid meets again.  The same steps as a training launch followed
 // by an Adam launch per slice, without their launches and per-launch
-// set-up.  acc: the grid barrier's counter (word ACC_BAR), zero at launch.
-constexpr int ACC_BAR = 0;
-constexpr int ACC_WORDS = 64;
+// set-up.  grid_bar: the grid barrier's arrival counter, zero at launch.
 constexpr uint32_t ADAM_SHARE = 128;  // parameters per CTA in the Adam phase (a multiple of 4)
 
 template <int SRC>
@@ -498,7 +495,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
                                                                float* __restrict__ adam_m, float* __restrict__ adam_v,
                                                                GuideSrc src, uint32_t chunk, uint32_t rounds,
                                                                float lr, float* __restrict__ part,
-                                                               float* __restrict__ loss_part, float* __restrict__ acc,
+                                                               float* __restrict__ loss_part, uint32_t* grid_bar,
                                                                float* __restrict__ loss_last, uint32_t* step_count,
                                                                uint32_t* status,
                                                                unsigned long long* __restrict__ sample_count) {
@@ -515,7 +512,6 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
   __shared__ __align__(16) float s_b[4 * 64 + 48];
   __shared__ float s_loss[4];
   const int tid = threadIdx.x, warp = tid >> 5;
-  uint32_t* counter = reinterpret_cast<uint32_t*>(acc + ACC_BAR);
   const uint32_t n = src.count ? min(*(volatile const uint32_t*)src.count, src.n) : src.n;
   const uint32_t t0 = *(volatile const uint32_t*)step_count;  // Adam steps before this launch
   if (tid == 0) {
@@ -587,7 +583,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
     });
     for (int k = tid; k < DB_WORDS; k += 128) slot[P_B + k] = ok ? bias_grad_total(s_db, s_loss, k) : 0.0f;
     if (tid == 0) loss_part[blockIdx.x] = ok ? bias_grad_total(s_db, s_loss, DB_WORDS) : 0.0f;
-    if (!grid_barrier(counter, bars++, status, &bar_ok) || failed) break;
+    if (!grid_barrier(grid_bar, bars++, status, &bar_ok) || failed) break;
     // Adam on this CTA's share (the step of k_guide_adam)
     const float t = (float)(t0 + done + 1);
     const float b1c = 1.0f - powf(0.9f, t), b2c = 1.0f - powf(0.999f, t);
@@ -643,7 +639,7 @@ __global__ void __launch_bounds__(128, 1) k_guide_train_rounds(uint16_t* __restr
     }
     asm volatile("fence.proxy.async.global;" ::: "memory");  // the pack, read next round by bulk copies
     ++done;
-    if (!grid_barrier(counter, bars++, status, &bar_ok)) break;
+    if (!grid_barrier(grid_bar, bars++, status, &bar_ok)) break;
   }
   if (blockIdx.x == 0 && tid == 0) {
     *step_count = t0 + done;
@@ -787,9 +783,9 @@ Status guide_launch_train(GuideNet& g, const GuideSrc& src, float inv_n, uint32_
 }
 
 // One wave's training rounds (k_guide_train_rounds), a cooperative launch
-// of one CTA per SM; acc (ACC_WORDS floats) is zeroed first.
+// of one CTA per SM; grid_bar (one word) is zeroed first.
 Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, int src_kind, uint32_t chunk, uint32_t rounds,
-                                 float lr, float* acc, cudaStream_t s, unsigned long long* sample_count) {
+                                 float lr, uint32_t* grid_bar, cudaStream_t s, unsigned long long* sample_count) {
   static bool attr_set = false;
   if (!attr_set) {
     LISA_CUDA(cudaFuncSetAttribute(k_guide_train_rounds<SRC_GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -798,7 +794,7 @@ Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, int src_kind,
                                    TRAIN_SMEM));
     attr_set = true;
   }
-  LISA_CUDA(cudaMemsetAsync(acc, 0, sizeof(float) * ACC_WORDS, s));
+  LISA_CUDA(cudaMemsetAsync(grid_bar, 0, sizeof(uint32_t), s));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)sm_count_current());
   cfg.blockDim = dim3(128);
@@ -812,16 +808,14 @@ Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, int src_kind,
   if (!g.grad_part) return Status::invalid("guide: no partial-gradient slots");  // one per SM
   if (src_kind == SRC_RAW)
     LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_RAW>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
-                                 chunk, rounds, lr, g.grad_part, g.loss_part, acc, g.loss_last, g.d_step, g.status,
+                                 chunk, rounds, lr, g.grad_part, g.loss_part, grid_bar, g.loss_last, g.d_step, g.status,
                                  sample_count));
   else
     LISA_CUDA(cudaLaunchKernelEx(&cfg, k_guide_train_rounds<SRC_GEOM>, g.w_bf16, g.master, g.adam_m, g.adam_v, src,
-                                 chunk, rounds, lr, g.grad_part, g.loss_part, acc, g.loss_last, g.d_step, g.status,
+                                 chunk, rounds, lr, g.grad_part, g.loss_part, grid_bar, g.loss_last, g.d_step, g.status,
                                  sample_count));
   return Status();
 }
-
-size_t guide_train_acc_words() { return ACC_WORDS; }
 
 // g.grads and g.loss = the sums of the last training launch's partials.
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s) {
@@ -881,7 +875,7 @@ Status guide_renderer_init(Renderer& r) {
   if (r.opts.estimator == LISA_ESTIMATOR_PHYSICAL)
     LISA_TRY(r.arena.alloc((void**)&r.nee_light, sizeof(float4) * 2ull * r.capacity, "emitter samples"));
   LISA_TRY(r.arena.alloc((void**)&r.guide_batch, sizeof(float4) * 4ull * B, "guide batch"));
-  LISA_TRY(r.arena.alloc((void**)&r.guide_acc, sizeof(float) * guide_train_acc_words(), "guide gradient sums"));
+  LISA_TRY(r.arena.alloc((void**)&r.guide_grid_bar, sizeof(uint32_t), "guide training barrier"));
   return Status();
 }
 
@@ -1042,12 +1036,13 @@ int lisa_guide_train_steps(lisa_guide* g, const float* features, const float* di
   if (n == 0 || steps == 0) return gret(Status::invalid("empty batch"));
   if (chunk == 0 || chunk % 128) return gret(Status::invalid("chunk must be a positive multiple of 128"));
   if (!(lr > 0.0f)) return gret(Status::invalid("lr must be positive"));
-  float *d_x = nullptr, *d_d = nullptr, *d_w = nullptr, *d_acc = nullptr;
+  float *d_x = nullptr, *d_d = nullptr, *d_w = nullptr;
+  uint32_t* d_bar = nullptr;
   auto run = [&]() -> Status {
     LISA_CUDA(cudaMalloc(&d_x, sizeof(float) * 64ull * n));
     LISA_CUDA(cudaMalloc(&d_d, sizeof(float) * 3ull * n));
     LISA_CUDA(cudaMalloc(&d_w, sizeof(float) * n));
-    LISA_CUDA(cudaMalloc(&d_acc, sizeof(float) * guide_train_acc_words()));
+    LISA_CUDA(cudaMalloc(&d_bar, sizeof(uint32_t)));
     LISA_CUDA(cudaMemcpyAsync(d_x, features, sizeof(float) * 64ull * n, cudaMemcpyHostToDevice, g->stream));
     LISA_CUDA(cudaMemcpyAsync(d_d, dirs, sizeof(float) * 3ull * n, cudaMemcpyHostToDevice, g->stream));
     LISA_CUDA(cudaMemcpyAsync(d_w, weights, sizeof(float) * n, cudaMemcpyHostToDevice, g->stream));
@@ -1057,7 +1052,7 @@ int lisa_guide_train_steps(lisa_guide* g, const float* features, const float* di
     src.dirs = d_d;
     src.weights = d_w;
     src.n = n;
-    LISA_TRY(guide_launch_train_rounds(g->get(), src, SRC_RAW, chunk, steps, lr, d_acc, g->stream, nullptr));
+    LISA_TRY(guide_launch_train_rounds(g->get(), src, SRC_RAW, chunk, steps, lr, d_bar, g->stream, nullptr));
     if (loss) LISA_CUDA(cudaMemcpyAsync(loss, g->get().loss_last, sizeof(float), cudaMemcpyDeviceToHost, g->stream));
     LISA_TRY(guide_check_status(g->get(), g->stream));
     return Status();
@@ -1066,7 +1061,7 @@ int lisa_guide_train_steps(lisa_guide* g, const float* features, const float* di
   if (d_x) cudaFree(d_x);
   if (d_d) cudaFree(d_d);
   if (d_w) cudaFree(d_w);
-  if (d_acc) cudaFree(d_acc);
+  if (d_bar) cudaFree(d_bar);
   return gret(s);
 }
 

@@ -71,11 +71,9 @@ Status guide_launch_infer(GuideNet& g, const GuideSrc& src, int src_kind, float*
 Status guide_launch_train(GuideNet& g, const GuideSrc& src, float inv_n, uint32_t max_n, cudaStream_t s,
                           bool adam_follows);
 // Up to `rounds` Adam steps on slices of `chunk` samples of src (RAW or
-// GEOM), in one cooperative launch; acc is scratch of
-// guide_train_acc_words() floats
+// GEOM), in one cooperative launch; grid_bar is one device word of scratch
 Status guide_launch_train_rounds(GuideNet& g, const GuideSrc& src, int src_kind, uint32_t chunk, uint32_t rounds,
-                                 float lr, float* acc, cudaStream_t s, unsigned long long* sample_count);
-size_t guide_train_acc_words();
+                                 float lr, uint32_t* grid_bar, cudaStream_t s, unsigned long long* sample_count);
 // g.grads / g.loss = sums of the last training launch's partials
 Status guide_launch_reduce(GuideNet& g, cudaStream_t s);
 // Adam step on the summed partials; also refreshes the BF16 weights and

@@ -220,7 +220,7 @@ struct Renderer {
   uint32_t guide_max_steps = 0;  // Adam steps after the largest wave
   float* guide_grad_part = nullptr;  // partial-gradient slots shared by the scenes' guides
   float* guide_loss_part = nullptr;
-  float* guide_acc = nullptr;        // gradient sums and grid barrier of the training rounds
+  uint32_t* guide_grid_bar = nullptr;  // the training rounds' grid-barrier counter
   uint64_t guide_waves_done = 0; // waves rendered in guided mode so far
   ~Renderer();
 };

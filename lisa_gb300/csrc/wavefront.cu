@@ -1481,7 +1481,7 @@ Status launch_wave_sequence(Renderer& r, const std::vector<WaveLaunch>& waves, l
       // one Adam step per slice of the collected samples, all in one
       // cooperative launch
       LISA_TRY(stage(5, [&] {
-        return guide_launch_train_rounds(*net, train_src, SRC_GEOM, r.guide_chunk, steps, r.opts.guide_lr, r.guide_acc,
+        return guide_launch_train_rounds(*net, train_src, SRC_GEOM, r.guide_chunk, steps, r.opts.guide_lr, r.guide_grid_bar,
                                          r.stream, &r.ctrl->train_samples);
       }));
     }
