@@ -199,6 +199,26 @@ def test_batch_render_one_call_writes_every_scene(gpu, tmp_path):
         assert (tmp_path / f"{name}.ppm").read_bytes() == want.read_bytes()
 
 
+def test_cli_renders_the_scene_file(gpu, tmp_path):
+    """`lisa -s scene.rto` (LiSA's main: parse, render, save_image) writes
+    the same PPM bytes as the library rendering the parsed scene."""
+    import os
+    import subprocess
+
+    sc = scenes.cornell_box(width=40, height=30, num_samples=8, num_bounces=5)
+    sc.output_image = str(tmp_path / "cli.ppm")
+    rto = scenes.write_rto(sc, str(tmp_path))
+    cli = os.path.join(os.path.dirname(L._native.LIB_PATH), "bin", "lisa")
+    run = subprocess.run([cli, "-s", rto, "--seed", "5"], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stderr
+    params = L.SceneParser(rto).get_params()
+    r = L.Renderer(params, seed=5)
+    r.render()
+    want = tmp_path / "lib.ppm"
+    r.save_image(str(want))
+    assert (tmp_path / "cli.ppm").read_bytes() == want.read_bytes()
+
+
 def test_cuda_graph_replay_matches_stream_launches(gpu):
     """The captured graph (reused across calls with the same wave shape,
     fresh wave table each call) gives the same image as direct launches."""
