@@ -80,7 +80,7 @@ def test_hard_indirect_guided_vs_plain(gpu, capsys):
     assert e_g <= 1.15 * e_p
 
 
-def test_guide_halves_time_to_plain_error(gpu, capsys):
+def test_guide_cuts_time_to_plain_error(gpu, capsys):
     """What the trained guide gains, at equal time.  The hard-indirect scene
     (the 1.31M-triangle displaced icosphere in the box, its light shrunk to
     0.02 x 0.02 behind a baffle), 1024 x 1024, 256 spp, 8 bounces,
@@ -88,7 +88,8 @@ def test_guide_halves_time_to_plain_error(gpu, capsys):
     4,096-spp plain reference accumulated in FP64, relMSE with the
     reference's own variance removed, device times measured by the
     renderer.  The guided render must reach the plain render's error in at
-    most 0.6 of the plain render's time (measured: about 0.27)."""
+    most 0.4 of the plain render's time (measured: 0.21-0.24 over seven
+    runs)."""
     import argparse
 
     from lisa_gb300 import study
@@ -101,7 +102,7 @@ def test_guide_halves_time_to_plain_error(gpu, capsys):
               f"{q['plain']['relmse_corrected']:.3e}, guided {q['guided']['ms']:.1f} ms relMSE "
               f"{q['guided']['relmse_corrected']:.3e}, time to plain's error {ratio:.3f}x")
     assert q["guided"]["guide_train"]["samples"] > 0 and q["guided"]["guide_infer"]["rows"] > 0
-    assert ratio is not None and ratio <= 0.6, ratio
+    assert ratio is not None and ratio <= 0.4, ratio
 
 
 def test_low_spp_scenes_render_plain_in_a_guided_batch(gpu):
