@@ -1,12 +1,15 @@
 // MLP path guide: fused tcgen05 kernels for inference, training (forward,
-// loss gradient, backward) and Adam.
+// loss gradient, backward) and Adam.  The renderer trains with
+// k_guide_train_rounds (every Adam round of a wave in one cooperative
+// launch); k_guide_train + k_guide_adam are the same steps as separate
+// launches, for the guide's own C ABI.
 //
 // Network: 64 encoded inputs -> 4 x (64, ReLU) -> 40 outputs = 8 vMF lobes
 // (guide_mix.cuh).  FP32 master weights; BF16 copies, pre-swizzled into the
 // K-major 128-byte-swizzle layout the UMMA descriptors expect, are copied
-// once per CTA into shared memory.  A CTA of 128 threads processes tiles of
-// 128 samples: thread t owns row t of every activation tile, and TMEM lane
-// t of every accumulator.  One elected thread issues tcgen05.mma (M = 128,
+// into each CTA's shared memory.  A training CTA of 128 threads processes
+// tiles of 128 samples: thread t owns row t of every activation tile, and
+// TMEM lane t of every accumulator.  One elected thread issues tcgen05.mma (M = 128,
 // K = 16 per instruction) and commits to an mbarrier; waits are bounded and
 // a time-out sets a status bit instead of hanging.
 //
