@@ -166,10 +166,11 @@ constexpr int INFER_BLOCKS_PER_SM = 2;
 //
 // The two warpgroups of a CTA run independent pipelines (named barriers,
 // one per warpgroup): thread 0 of a warpgroup issues its tile's layer
-// (tcgen05.mma, M = 128, K = 16 per instruction) and waits for it on the
-// warpgroup's mbarrier; the warpgroup meets at its barrier, every thread
-// reads its accumulator row with tcgen05.ld and writes the next layer's
-// input row (bias, ReLU, BF16) over the tile in shared memory.  While one
+// (tcgen05.mma, M = 128, K = 16 per instruction), every thread of the
+// warpgroup waits for it on the warpgroup's mbarrier, reads its
+// accumulator row with tcgen05.ld and writes the next layer's input row
+// (bias, ReLU, BF16) over the tile in shared memory, and the warpgroup
+// meets at its barrier before the next issue.  While one
 // warpgroup runs an epilogue, the tensor core runs the other warpgroups'
 // layers.
 template <int SRC, class Pre, class Epi>
@@ -214,13 +215,14 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   uint8_t* const act = smem + FWD_BYTES + 16384 * wg;
   const uint32_t bar_id = 1u + wg;
   auto wg_sync = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(bar_id) : "memory"); };
-  // thread 0 of the warpgroup: parity of the next completion, and whether a
-  // committed MMA has not been waited for
-  uint32_t phase = 0;
+  // parity of the warpgroup's next MMA completion; thread 0 of the
+  // warpgroup: whether a committed MMA has not been waited for, and its parity
+  uint32_t phase = 0, busy_parity = 0;
   bool busy = false;
   auto issue = [&](int l) {
     issue_layer(tmem, act, w + (l < 4 ? (R_FWD + 64 * l) : R_W5) * 128, l < 4 ? 64u : 48u, &mbar[wg]);
     busy = true;
+    busy_parity = phase;
   };
   for (uint32_t tile = 2 * blockIdx.x + wg; tile < ntiles; tile += 2 * gridDim.x) {
     if (failed[wg]) break;  // read after a warpgroup barrier: uniform over the warpgroup
@@ -246,18 +248,17 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
     if (t == 0) issue(0);
 #pragma unroll 1
     for (int l = 0; l < 5; ++l) {
-      if (t == 0) {
-        if (tc::mbar_wait(&mbar[wg], phase)) {
-          phase ^= 1u;
-          busy = false;
-        } else {
-          atomicOr(status, ST_GUIDE_NONFINITE << 1);
-          failed[wg] = 1;
-        }
+      // every thread waits for the layer's MMA itself (bounded; no barrier
+      // to hand the completion on); a time-out reaches the others through
+      // failed[wg] at the warpgroup's next barrier
+      if (tc::mbar_wait(&mbar[wg], phase)) {
+        if (t == 0) busy = false;
+      } else {
+        atomicOr(status, ST_GUIDE_NONFINITE << 1);
+        failed[wg] = 1;
       }
-      wg_sync();  // the others learn of the finished MMA here
+      phase ^= 1u;
       tc::fence_after_sync();
-      if (failed[wg]) break;
       float acc[64];
       if (l < 4) {
         tc::tmem_ld16x<4>(lane_addr, acc);
@@ -266,6 +267,7 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
         tc::fence_before_sync();
         wg_sync();
         tc::fence_after_sync();
+        if (failed[wg]) break;
         if (t == 0) issue(l + 1);
       } else {
         tc::tmem_ld16x<3>(lane_addr, acc);
@@ -281,7 +283,7 @@ __device__ __forceinline__ void infer_tiles(const uint16_t* __restrict__ pack, c
   }
   // after a time-out, give an MMA still in flight a bounded chance to finish
   // before its TMEM is freed
-  if (t == 0 && busy) tc::mbar_wait(&mbar[wg], phase, 1u << 20);
+  if (t == 0 && busy) tc::mbar_wait(&mbar[wg], busy_parity, 1u << 20);
   if (tid == 0 && weights_failed) tc::mbar_wait(&mbar_w, 0, 1u << 20);  // a late weight copy
   tc::fence_before_sync();
   __syncthreads();
